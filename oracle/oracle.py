@@ -1,0 +1,278 @@
+"""ctypes bindings for the CPU oracles.  TEST INFRASTRUCTURE ONLY.
+
+Two libraries, both built by oracle/Makefile:
+  * _build/libnsm_oracle.so -- the plain-C restatement (nsm_oracle.c), built on
+    every machine (it is the CPU baseline "port" where the reference is absent);
+  * _ref/libnimble_ref.so   -- NimbleSM's own host sources plus ref_harness.cc,
+    buildable only where the reference sources are present.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline legs import
+this module, as the checker or as the timed CPU baseline.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PORT_SO = os.path.join(HERE, "_build", "libnsm_oracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libnimble_ref.so")
+REF_SRC = "/root/reference/src"
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+
+
+def _d(a):
+    return None if a is None else a.ctypes.data_as(_dp)
+
+
+def _i(a):
+    return None if a is None else a.ctypes.data_as(_ip)
+
+
+def build(ref: bool | None = None) -> None:
+    """Builds the C restatement, and the reference library when its sources
+    are present (or when ref=True)."""
+    subprocess.run(["make", "-s", "-C", HERE, "port"], check=True)
+    if ref is None:
+        ref = os.path.isdir(REF_SRC)
+    if ref:
+        subprocess.run(["make", "-s", "-j8", "-C", HERE, "ref"], check=True)
+
+
+class _Model(C.Structure):
+    _fields_ = [
+        ("num_nodes", C.c_int), ("num_elem", C.c_int), ("coords", _dp), ("conn", _ip),
+        ("density", C.c_double), ("bulk_modulus", C.c_double), ("shear_modulus", C.c_double),
+        ("num_bcs", C.c_int), ("bc_kind", _ip), ("bc_component", _ip), ("bc_value", _dp),
+        ("bc_ptr", _ip), ("bc_nodes", _ip),
+    ]
+
+
+class _Result(C.Structure):
+    _fields_ = [
+        ("u", _dp), ("v", _dp), ("a", _dp), ("f_int", _dp), ("F", _dp), ("sigma", _dp), ("mass", _dp),
+        ("dt_crit", C.c_double), ("kinetic_energy", C.c_double), ("internal_energy", C.c_double),
+        ("loop_seconds", C.c_double),
+    ]
+
+
+_port = None
+_ref = None
+
+
+def port():
+    global _port
+    if _port is None:
+        if not os.path.exists(PORT_SO):
+            build(ref=False)
+        lib = C.CDLL(PORT_SO)
+        lib.nsm_oracle_run.argtypes = [C.POINTER(_Model), C.c_double, C.c_int, C.c_int, _dp, C.c_int,
+                                       C.POINTER(_Result)]
+        lib.nsm_oracle_continue.argtypes = [C.POINTER(_Model), C.c_double, C.c_double, C.c_int, C.c_int,
+                                            _dp, _dp, _dp, _dp]
+        lib.nsm_oracle_element.argtypes = [_dp, _dp, C.c_double, C.c_double, _dp, _dp, _dp]
+        lib.nsm_oracle_stress.argtypes = [C.c_int, _dp, C.c_double, C.c_double, _dp]
+        lib.nsm_oracle_lumped_mass.argtypes = [C.POINTER(_Model), _dp]
+        lib.nsm_oracle_critical_time_step.argtypes = [C.POINTER(_Model)]
+        lib.nsm_oracle_critical_time_step.restype = C.c_double
+        lib.nsm_oracle_energy_density.argtypes = [_dp, C.c_double, C.c_double]
+        lib.nsm_oracle_energy_density.restype = C.c_double
+        lib.nsm_oracle_shape_tables.argtypes = [_dp, _dp]
+        lib.nsm_oracle_create.argtypes = [C.POINTER(_Model), C.c_int]
+        lib.nsm_oracle_create.restype = C.c_void_p
+        lib.nsm_oracle_destroy.argtypes = [C.c_void_p]
+        lib.nsm_oracle_dt_crit.argtypes = [C.c_void_p]
+        lib.nsm_oracle_dt_crit.restype = C.c_double
+        lib.nsm_oracle_begin.argtypes = [C.c_void_p, C.c_double, C.c_int, C.c_int, _dp]
+        lib.nsm_oracle_advance.argtypes = [C.c_void_p, C.c_int, _dp]
+        lib.nsm_oracle_time.argtypes = [C.c_void_p]
+        lib.nsm_oracle_time.restype = C.c_double
+        lib.nsm_oracle_get_state.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp, _dp, _dp, _dp]
+        lib.nsm_oracle_set_state.argtypes = [C.c_void_p, _dp, _dp, _dp]
+        lib.nsm_oracle_energies.argtypes = [C.c_void_p, _dp, _dp]
+        _port = lib
+    return _port
+
+
+def reference_available() -> bool:
+    return os.path.exists(REF_SO)
+
+
+def ref():
+    global _ref
+    if _ref is None:
+        if not os.path.exists(REF_SO):
+            raise RuntimeError("reference library not built (oracle/_ref); needs the reference sources")
+        lib = C.CDLL(REF_SO)
+        lib.nimref_run.argtypes = [C.c_int, _dp, C.c_int, _ip, C.c_int, _ip, _ip, C.c_char_p, C.c_char_p,
+                                   C.c_char_p, C.c_double, C.c_int, C.c_int, _dp,
+                                   _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp]
+        lib.nimref_element.argtypes = [_dp, _dp, C.c_double, C.c_double, C.c_double, _dp, _dp, _dp]
+        lib.nimref_stress.argtypes = [C.c_int, _dp, C.c_double, C.c_double, _dp]
+        lib.nimref_last_error.restype = C.c_char_p
+        _ref = lib
+    return _ref
+
+
+def _model(problem, keep):
+    kinds, comps, vals, ptr, nodes = problem.bc_arrays()
+    coords = np.ascontiguousarray(problem.coords, dtype=np.float64)
+    conn = np.ascontiguousarray(problem.conn, dtype=np.int32)
+    keep.extend([kinds, comps, vals, ptr, nodes, coords, conn])
+    return _Model(problem.num_nodes, problem.num_elem, _d(coords), _i(conn), problem.density,
+                  problem.bulk_modulus, problem.shear_modulus, len(kinds), _i(kinds), _i(comps), _d(vals),
+                  _i(ptr), _i(nodes))
+
+
+def _outputs(problem, with_ip):
+    N, E = problem.num_nodes, problem.num_elem
+    out = {k: np.zeros((N, 3)) for k in ("u", "v", "a", "f_int")}
+    out["mass"] = np.zeros(N)
+    if with_ip:
+        out["F"] = np.zeros((E, 8, 9))
+        out["sigma"] = np.zeros((E, 8, 6))
+    return out
+
+
+def run_port(problem, final_time, num_steps, output_frequency=0, threads=1, with_ip=True):
+    """Runs the C restatement; returns a dict of numpy arrays and scalars."""
+    keep = []
+    m = _model(problem, keep)
+    out = _outputs(problem, with_ip)
+    res = _Result(_d(out["u"]), _d(out["v"]), _d(out["a"]), _d(out["f_int"]), _d(out.get("F")),
+                  _d(out.get("sigma")), _d(out["mass"]), 0.0, 0.0, 0.0, 0.0)
+    v0 = None if problem.v_init is None else np.ascontiguousarray(problem.v_init, dtype=np.float64)
+    rc = port().nsm_oracle_run(C.byref(m), float(final_time), int(num_steps), int(output_frequency),
+                               _d(v0), int(threads), C.byref(res))
+    if rc != 0:
+        raise RuntimeError(f"oracle run failed ({rc}): non-positive Jacobian")
+    out.update(dt_crit=res.dt_crit, kinetic_energy=res.kinetic_energy,
+               internal_energy=res.internal_energy, loop_seconds=res.loop_seconds)
+    return out
+
+
+class PortRun:
+    """Stateful run of the C restatement: begin(), advance(k), state()."""
+
+    def __init__(self, problem, threads=1):
+        self.problem = problem
+        self._keep = []
+        self._model = _model(problem, self._keep)
+        self._h = port().nsm_oracle_create(C.byref(self._model), int(threads))
+        if not self._h:
+            raise MemoryError("oracle allocation failed")
+        self.dt_crit = port().nsm_oracle_dt_crit(self._h)
+
+    def begin(self, final_time, num_steps, output_frequency=0):
+        v0 = None if self.problem.v_init is None else np.ascontiguousarray(self.problem.v_init, np.float64)
+        self._keep.append(v0)
+        port().nsm_oracle_begin(self._h, float(final_time), int(num_steps), int(output_frequency), _d(v0))
+
+    def advance(self, k):
+        secs = C.c_double(0.0)
+        if port().nsm_oracle_advance(self._h, int(k), C.cast(C.pointer(secs), _dp)) != 0:
+            raise RuntimeError("oracle step failed: non-positive Jacobian")
+        return secs.value
+
+    def state(self, with_ip=True):
+        out = _outputs(self.problem, with_ip)
+        port().nsm_oracle_get_state(self._h, _d(out["u"]), _d(out["v"]), _d(out["a"]), _d(out["f_int"]),
+                                    _d(out.get("F")), _d(out.get("sigma")), _d(out["mass"]))
+        out["time"] = port().nsm_oracle_time(self._h)
+        ke, ie = C.c_double(0.0), C.c_double(0.0)
+        port().nsm_oracle_energies(self._h, C.cast(C.pointer(ke), _dp), C.cast(C.pointer(ie), _dp))
+        out["kinetic_energy"], out["internal_energy"] = ke.value, ie.value
+        return out
+
+    def set_state(self, u=None, v=None, a=None):
+        arrs = [None if x is None else np.ascontiguousarray(x, np.float64) for x in (u, v, a)]
+        port().nsm_oracle_set_state(self._h, *[_d(x) for x in arrs])
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            port().nsm_oracle_destroy(self._h)
+            self._h = None
+
+
+def continue_port(problem, u, v, a, t0, dt, num_steps, threads):
+    """Advances (u, v, a) in place by num_steps with a fixed step; returns the
+    wall seconds of the step loop."""
+    keep = []
+    m = _model(problem, keep)
+    secs = C.c_double(0.0)
+    rc = port().nsm_oracle_continue(C.byref(m), float(t0), float(dt), int(num_steps), int(threads),
+                                    _d(u), _d(v), _d(a), C.cast(C.pointer(secs), _dp))
+    if rc != 0:
+        raise RuntimeError(f"oracle continue failed ({rc})")
+    return secs.value
+
+
+def run_ref(problem, final_time, num_steps, output_frequency=0, with_ip=True):
+    """Runs the reference itself (oracle/_ref); same outputs as run_port."""
+    lib = ref()
+    kinds, comps, vals, ptr, nodes = problem.bc_arrays()
+    names = list(problem.node_sets.keys())
+    ns_ptr = np.zeros(len(names) + 1, np.int32)
+    parts = []
+    for s, nm in enumerate(names):
+        ids = np.asarray(problem.node_sets[nm], np.int32)
+        parts.append(ids)
+        ns_ptr[s + 1] = ns_ptr[s] + len(ids)
+    ns_nodes = np.concatenate(parts).astype(np.int32) if parts else np.zeros(0, np.int32)
+    bcs = "\n".join(bc.line() for bc in problem.bcs)
+    out = _outputs(problem, with_ip)
+    coords = np.ascontiguousarray(problem.coords, dtype=np.float64)
+    conn = np.ascontiguousarray(problem.conn, dtype=np.int32)
+    v0 = None if problem.v_init is None else np.ascontiguousarray(problem.v_init, dtype=np.float64)
+    dt = C.c_double(0.0)
+    secs = C.c_double(0.0)
+    rc = lib.nimref_run(problem.num_nodes, _d(coords), problem.num_elem, _i(conn), len(names), _i(ns_ptr),
+                        _i(ns_nodes), "\n".join(names).encode(), problem.material_line().encode(),
+                        bcs.encode(), float(final_time), int(num_steps), int(output_frequency), _d(v0),
+                        _d(out["u"]), _d(out["v"]), _d(out["a"]), _d(out["f_int"]), _d(out.get("F")),
+                        _d(out.get("sigma")), _d(out["mass"]), C.cast(C.pointer(dt), _dp),
+                        C.cast(C.pointer(secs), _dp))
+    if rc != 0:
+        raise RuntimeError("reference run failed: " + lib.nimref_last_error().decode())
+    out.update(dt_crit=dt.value, loop_seconds=secs.value)
+    return out
+
+
+def element(X, u, K, G, which="port"):
+    """One element (X, u: [8,3]) -> (F [8,9], sigma [8,6], f [8,3])."""
+    X = np.ascontiguousarray(X, dtype=np.float64)
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    F, s, f = np.zeros((8, 9)), np.zeros((8, 6)), np.zeros((8, 3))
+    if which == "port":
+        port().nsm_oracle_element(_d(X), _d(u), K, G, _d(F), _d(s), _d(f))
+    else:
+        if ref().nimref_element(_d(X), _d(u), 1.0, K, G, _d(F), _d(s), _d(f)) != 0:
+            raise RuntimeError(ref().nimref_last_error().decode())
+    return F, s, f
+
+
+def stress(F, K, G, which="port"):
+    F = np.ascontiguousarray(F, dtype=np.float64).reshape(-1, 9)
+    s = np.zeros((F.shape[0], 6))
+    if which == "port":
+        port().nsm_oracle_stress(F.shape[0], _d(F), K, G, _d(s))
+    else:
+        if ref().nimref_stress(F.shape[0], _d(F), K, G, _d(s)) != 0:
+            raise RuntimeError(ref().nimref_last_error().decode())
+    return s
+
+
+def shape_tables():
+    N, dN = np.zeros((8, 8)), np.zeros((8, 8, 3))
+    port().nsm_oracle_shape_tables(_d(N), _d(dN))
+    return N, dN
+
+
+def energy_density(F, K, G):
+    F = np.ascontiguousarray(F, dtype=np.float64)
+    return port().nsm_oracle_energy_density(_d(F), K, G)

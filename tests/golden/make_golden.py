@@ -1,0 +1,244 @@
+"""Generates the golden fixtures in tests/golden/ (run in a container that has
+the NimbleSM sources; the fixtures are committed so the tests need neither the
+sources nor the reference build).
+
+Two kinds of fixture:
+  * gold_*.npz -- the reference's own regression gold files
+    (test/dynamics/**/.gold.e, NetCDF-3, read with scipy), with the mesh they
+    were made from (.g), the deck's material and boundary conditions (.in) and
+    the per-variable exodiff tolerances (.exodiff).
+  * ref_*.npz  -- outputs of the reference itself (oracle/_ref, NimbleSM's host
+    sources compiled from where they lie) on seeded synthetic inputs.
+
+Usage: python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import os
+import re
+import sys
+
+import numpy as np
+import scipy.io
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from nimblesm_gb300.mesh import (CORNER_SIGNS, BoundaryCondition, Problem, cube_problem,  # noqa: E402
+                                 critical_time_step)
+from oracle import oracle as O  # noqa: E402
+
+REF = "/root/reference"
+
+
+def _names(var):
+    return [b"".join(r).strip(b"\x00").decode() for r in var[:]]
+
+
+def read_exodus(path):
+    """Mesh and results of an Exodus II (NetCDF-3) file: 0-based connectivity
+    of block 1, node sets named nodelist_<id> when unnamed (as
+    src/nimble_genesis_mesh.cc:160-172 does), nodal and element variables."""
+    d = scipy.io.netcdf_file(path, "r", mmap=False)
+    v = d.variables
+    coords = np.stack([v["coordx"][:], v["coordy"][:], v["coordz"][:]], axis=1).astype(np.float64)
+    conn = v["connect1"][:].astype(np.int32) - 1
+    ns = {}
+    if "ns_prop1" in v:
+        names = _names(v["ns_names"]) if "ns_names" in v else [""] * len(v["ns_prop1"][:])
+        for k, sid in enumerate(v["ns_prop1"][:]):
+            nm = names[k] or f"nodelist_{int(sid)}"
+            ns[nm] = v[f"node_ns{k + 1}"][:].astype(np.int32) - 1
+    out = {"coords": coords, "conn": conn, "node_sets": ns}
+    if "time_whole" in v:
+        out["times"] = v["time_whole"][:].astype(np.float64)
+        if "name_nod_var" in v:
+            for k, nm in enumerate(_names(v["name_nod_var"])):
+                out["nod:" + nm] = v[f"vals_nod_var{k + 1}"][:].astype(np.float64)
+        if "name_elem_var" in v:
+            for k, nm in enumerate(_names(v["name_elem_var"])):
+                key = f"vals_elem_var{k + 1}eb1"
+                if key in v:
+                    out["elem:" + nm] = v[key][:].astype(np.float64)
+    d.close()
+    return out
+
+
+def read_deck(path):
+    """Material parameters and boundary-condition lines of an input deck."""
+    mat, bcs, keys = None, [], {}
+    for line in open(path):
+        line = line.split("#")[0].strip()
+        if ":" not in line:
+            continue
+        k, val = (s.strip() for s in line.split(":", 1))
+        if k == "material parameters":
+            mat = val.split()
+        elif k == "boundary condition":
+            bcs.append(val)
+        else:
+            keys[k] = val
+    params = {mat[i]: float(mat[i + 1]) for i in range(2, len(mat) - 1, 2)}
+    return params, bcs, keys
+
+
+def read_exodiff(path):
+    """Per-variable absolute tolerances of an exodiff command file."""
+    tol = {}
+    for line in open(path):
+        m = re.match(r"\s+(\w+)\s+absolute\s+([0-9.eE+-]+)", line)
+        if m:
+            tol[m.group(1)] = float(m.group(2))
+    return tol
+
+
+_VEC = ("x", "y", "z")
+# Reference component order -> Exodus component names (src/nimble_data_utils.cc:158-207).
+_FULL = ("xx", "yy", "zz", "xy", "yz", "zx", "yx", "zy", "xz")
+_SYM = ("xx", "yy", "zz", "xy", "yz", "zx")
+
+
+def gold_fixture(name, deck_dir, deck, genesis, gold, exodiff):
+    base = os.path.join(REF, "test", "dynamics", deck_dir)
+    mesh = read_exodus(os.path.join(base, genesis))
+    res = read_exodus(os.path.join(base, gold))
+    params, bc_lines, keys = read_deck(os.path.join(base, deck))
+    tol = read_exodiff(os.path.join(base, exodiff))
+    assert np.array_equal(mesh["coords"], res["coords"]), "gold file nodes are in mesh order"
+    T = len(res["times"])
+    N, E = mesh["coords"].shape[0], mesh["conn"].shape[0]
+    fx = {
+        "coords": mesh["coords"], "conn": mesh["conn"], "times": res["times"],
+        "ns_names": np.array(list(mesh["node_sets"].keys())),
+        "density": params["density"], "bulk_modulus": params["bulk_modulus"],
+        "shear_modulus": params["shear_modulus"], "bc_lines": np.array(bc_lines),
+        "final_time": float(keys["final time"]), "num_steps": int(keys["number of load steps"]),
+        "output_frequency": int(keys.get("output frequency", "1")),
+    }
+    for nm, ids in mesh["node_sets"].items():
+        fx["ns:" + nm] = ids
+    for field in ("displacement", "velocity", "acceleration", "internal_force"):
+        if "nod:" + field + "_x" in res:
+            fx["gold:" + field] = np.stack([res[f"nod:{field}_{c}"] for c in _VEC], axis=2)  # [T,N,3]
+            fx["tol:" + field] = np.array([tol.get(f"{field}_{c}", 0.0) for c in _VEC])
+    F = np.zeros((T, E, 8, 9))
+    S = np.zeros((T, E, 8, 6))
+    tF = np.zeros((8, 9))
+    tS = np.zeros((8, 6))
+    for ip in range(8):
+        for c, nm in enumerate(_FULL):
+            key = f"ipt{ip + 1:02d}_deformation_gradient_{nm}"
+            F[:, :, ip, c] = res["elem:" + key]
+            tF[ip, c] = tol.get(key, 0.0)
+        for c, nm in enumerate(_SYM):
+            key = f"ipt{ip + 1:02d}_stress_{nm}"
+            S[:, :, ip, c] = res["elem:" + key]
+            tS[ip, c] = tol.get(key, 0.0)
+    fx["gold:F"], fx["gold:sigma"], fx["tol:F"], fx["tol:sigma"] = F, S, tF, tS
+    np.savez_compressed(os.path.join(HERE, f"gold_{name}.npz"), **fx)
+    print("wrote", name, {k: np.shape(v) for k, v in fx.items() if k.startswith("gold")})
+
+
+def problem_from_fixture(fx) -> Problem:
+    names = [str(s) for s in fx["ns_names"]]
+    return Problem(coords=fx["coords"], conn=fx["conn"], node_sets={n: fx["ns:" + n] for n in names},
+                   density=float(fx["density"]), bulk_modulus=float(fx["bulk_modulus"]),
+                   shear_modulus=float(fx["shear_modulus"]),
+                   bcs=[BoundaryCondition.parse(str(b)) for b in fx["bc_lines"]])
+
+
+def ref_cube_fixture(name, n, jitter, seed, steps, output_frequency, sample_elems=None):
+    p = cube_problem(n, jitter=jitter, seed=seed)
+    dt = 0.5 * critical_time_step(p)
+    final_time = steps * dt
+    r = O.run_ref(p, final_time, steps, output_frequency)
+    fx = {"n": n, "jitter": jitter, "seed": seed, "steps": steps, "output_frequency": output_frequency,
+          "final_time": final_time, "dt_crit": r["dt_crit"]}
+    for k in ("u", "v", "a", "f_int", "mass"):
+        fx[k] = r[k]
+    if sample_elems is None:
+        fx["F"], fx["sigma"] = r["F"], r["sigma"]
+    else:
+        rng = np.random.default_rng(12345)
+        idx = np.sort(rng.choice(p.num_elem, sample_elems, replace=False))
+        fx["elem_index"] = idx
+        fx["F"], fx["sigma"] = r["F"][idx], r["sigma"][idx]
+        fx["F_norm"] = np.linalg.norm(r["F"])
+        fx["sigma_norm"] = np.linalg.norm(r["sigma"])
+    np.savez_compressed(os.path.join(HERE, f"ref_{name}.npz"), **fx)
+    print("wrote", name, r["loop_seconds"], "s")
+
+
+def ref_points_fixture():
+    """Stress and single-element known answers from the reference."""
+    rng = np.random.default_rng(2024)
+    K, G = 160e9, 79.3e9
+    Fs = []
+    for scale in (1e-6, 1e-4, 1e-3, 1e-2, 5e-2, 0.2):
+        for _ in range(16):
+            H = rng.normal(0.0, scale, size=(3, 3))
+            M = np.eye(3) + H
+            # reference storage order xx,yy,zz,xy,yz,zx,yx,zy,xz
+            Fs.append([M[0, 0], M[1, 1], M[2, 2], M[0, 1], M[1, 2], M[2, 0], M[1, 0], M[2, 1], M[0, 2]])
+    Fs.append([1.0, 1.0, 1.0, 0, 0, 0, 0, 0, 0])  # identity: the eigen solver's degenerate branch
+    Fs = np.array(Fs)
+    sig = O.stress(Fs, K, G, which="ref")
+    X0 = CORNER_SIGNS.astype(np.float64)
+    Xs, Us, Fe, Se, fe = [], [], [], [], []
+    for k in range(24):
+        h = 10.0 ** rng.uniform(-3, 0)
+        X = 0.5 * h * X0 + rng.uniform(-0.15 * h, 0.15 * h, size=(8, 3)) + rng.uniform(-1, 1, size=3)
+        U = rng.normal(0.0, h * 10.0 ** rng.uniform(-5, -1.5), size=(8, 3))
+        F, S, f = O.element(X, U, K, G, which="ref")
+        Xs.append(X), Us.append(U), Fe.append(F), Se.append(S), fe.append(f)
+    np.savez_compressed(os.path.join(HERE, "ref_points.npz"), K=K, G=G, F=Fs, sigma=sig, elem_X=np.array(Xs),
+                        elem_u=np.array(Us), elem_F=np.array(Fe), elem_sigma=np.array(Se), elem_f=np.array(fe))
+    print("wrote points", Fs.shape)
+
+
+def ref_gold_rerun():
+    """The reference itself on the gold decks, every output time, bitwise."""
+    for name in ("single_elem_native_neohookean", "wave_in_bar"):
+        fx = dict(np.load(os.path.join(HERE, f"gold_{name}.npz")))
+        p = problem_from_fixture(fx)
+        steps, of = int(fx["num_steps"]), int(fx["output_frequency"])
+        out_steps = [s + 1 for s in range(steps) if of != 0 and (s % of == 0 or s == steps - 1)]
+        res = {"out_steps": np.array(out_steps)}
+        for k in ("u", "v", "a", "f_int", "F", "sigma"):
+            res[k] = []
+        # Each output state is the end of a run truncated at that step with the
+        # same time step: final_time is scaled so dt_user is unchanged only when
+        # exact; the full schedule is rerun instead to keep dt identical.
+        for s_end in out_steps:
+            r = _ref_run_until(p, float(fx["final_time"]), steps, of, s_end)
+            for k in ("u", "v", "a", "f_int", "F", "sigma"):
+                res[k].append(r[k])
+        np.savez_compressed(os.path.join(HERE, f"ref_{name}.npz"), **{k: np.array(v) for k, v in res.items()})
+        print("wrote ref rerun", name, out_steps)
+
+
+def _ref_run_until(p, final_time, steps, of, s_end):
+    """Reference run of the deck's schedule stopped after s_end steps.  The
+    harness runs whole schedules, so the schedule is rerun with num_steps =
+    s_end and final_time = s_end * dt_user; this keeps dt_user bitwise equal
+    when final_time/steps*s_end/s_end rounds back, which is checked."""
+    dt_user = final_time / steps
+    ft = dt_user * s_end
+    assert ft / s_end == dt_user, "truncated schedule would change the time step"
+    # Output steps of the truncated run must match the full run's up to s_end.
+    r = O.run_ref(p, ft, s_end, of)
+    return r
+
+
+if __name__ == "__main__":
+    O.build(ref=True)
+    gold_fixture("single_elem_native_neohookean", "single_elem_complex_displacement",
+                 "single_elem_native_neohookean.in", "single_elem.g", "single_elem_native_neohookean.gold.e",
+                 "single_elem_native_neohookean.exodiff")
+    gold_fixture("wave_in_bar", "wave_in_bar", "wave_in_bar.in", "wave_in_bar.g", "wave_in_bar.gold.e",
+                 "wave_in_bar.exodiff")
+    ref_points_fixture()
+    ref_cube_fixture("cube4_jitter", 4, 0.2, 7, 20, 0)
+    ref_cube_fixture("cube16_cfg0", 16, 0.0, 0, 500, 500, sample_elems=64)
+    ref_gold_rerun()

@@ -1,0 +1,116 @@
+"""The CPU oracle (oracle/nsm_oracle.c) pinned against the reference: its gold
+files at the exodiff tolerances, and the reference's own outputs bit for bit."""
+import numpy as np
+import pytest
+
+from nimblesm_gb300.mesh import cube_problem, critical_time_step
+from oracle import oracle as O
+from tests.goldens import exodiff_ok, gold_problem, load, output_steps
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _build():
+    O.build(ref=False)
+
+
+def test_points_match_reference_bitwise():
+    fx = load("ref_points")
+    s = O.stress(fx["F"], float(fx["K"]), float(fx["G"]))
+    assert np.array_equal(s, fx["sigma"])
+    for k in range(fx["elem_X"].shape[0]):
+        F, S, f = O.element(fx["elem_X"][k], fx["elem_u"][k], float(fx["K"]), float(fx["G"]))
+        assert np.array_equal(F, fx["elem_F"][k])
+        assert np.array_equal(S, fx["elem_sigma"][k])
+        assert np.array_equal(f, fx["elem_f"][k])
+
+
+def test_identity_stress_is_zero():
+    F = np.array([[1.0, 1.0, 1.0, 0, 0, 0, 0, 0, 0]])
+    assert np.all(O.stress(F, 160e9, 79.3e9) == 0.0)
+
+
+@pytest.mark.parametrize("name", ["cube4_jitter", "cube16_cfg0"])
+def test_cube_runs_match_reference_bitwise(name):
+    fx = load("ref_" + name)
+    p = cube_problem(int(fx["n"]), jitter=float(fx["jitter"]), seed=int(fx["seed"]))
+    r = O.run_port(p, float(fx["final_time"]), int(fx["steps"]), int(fx["output_frequency"]), threads=4)
+    assert r["dt_crit"] == float(fx["dt_crit"])
+    for k in ("u", "v", "a", "f_int", "mass"):
+        assert np.array_equal(r[k], fx[k]), k
+    idx = fx.get("elem_index")
+    F, S = (r["F"], r["sigma"]) if idx is None else (r["F"][idx], r["sigma"][idx])
+    assert np.array_equal(F, fx["F"]) and np.array_equal(S, fx["sigma"])
+    if idx is not None:
+        assert np.linalg.norm(r["F"]) == float(fx["F_norm"])
+        assert np.linalg.norm(r["sigma"]) == float(fx["sigma_norm"])
+
+
+def test_numpy_critical_time_step_matches_oracle():
+    p = cube_problem(6, jitter=0.2, seed=11)
+    keep = []
+    assert critical_time_step(p) == O.PortRun(p).dt_crit
+
+
+@pytest.mark.parametrize("name", ["single_elem_native_neohookean", "wave_in_bar"])
+def test_gold_files(name):
+    """The reference's regression decks against their gold files, at the
+    exodiff tolerances, at every output time; and bit for bit against the
+    reference run here on the same deck."""
+    fx = load("gold_" + name)
+    rf = load("ref_" + name)
+    p = gold_problem(fx)
+    steps, of = int(fx["num_steps"]), int(fx["output_frequency"])
+    run = O.PortRun(p)
+    run.begin(float(fx["final_time"]), steps, of)
+    done = 0
+    for t_index, s_end in enumerate(output_steps(steps, of)):
+        run.advance(s_end - done)
+        done = s_end
+        st = run.state()
+        assert np.isclose(st["time"], fx["times"][t_index + 1], rtol=1e-12, atol=0)
+        for field, key in (("displacement", "u"), ("velocity", "v"), ("acceleration", "a"),
+                           ("internal_force", "f_int")):
+            if "gold:" + field in fx:
+                assert exodiff_ok(st[key], fx["gold:" + field][t_index + 1], fx["tol:" + field]), field
+        assert exodiff_ok(st["F"], fx["gold:F"][t_index + 1], fx["tol:F"])
+        assert exodiff_ok(st["sigma"], fx["gold:sigma"][t_index + 1], fx["tol:sigma"])
+        # the reference itself, same deck, same machine arithmetic
+        for key in ("u", "v", "a", "f_int", "F", "sigma"):
+            assert np.array_equal(st[key], rf[key][t_index]), key
+
+
+def test_thread_count_does_not_change_results():
+    p = cube_problem(5, jitter=0.2, seed=5)
+    dt = 0.5 * critical_time_step(p)
+    a = O.run_port(p, 30 * dt, 30, 0, threads=1)
+    b = O.run_port(p, 30 * dt, 30, 0, threads=3)
+    for k in ("u", "v", "a", "f_int", "F", "sigma"):
+        assert np.array_equal(a[k], b[k])
+
+
+def test_energy_is_bounded_to_integration_error():
+    """KE + IE oscillates (central difference conserves a modified energy, and
+    fixed nodes carry half a step of reaction velocity between output steps)
+    but does not drift."""
+    p = cube_problem(6, jitter=0.2, seed=1)
+    dt = 0.5 * critical_time_step(p)
+    run = O.PortRun(p)
+    run.begin(400 * dt, 400, 0)
+    run.advance(1)
+    e0 = run.state()
+    tot0 = e0["kinetic_energy"] + e0["internal_energy"]
+    for _ in range(8):
+        run.advance(50)
+        e = run.state()
+        assert e["internal_energy"] > 0
+        assert abs(e["kinetic_energy"] + e["internal_energy"] - tot0) / tot0 < 5e-2
+
+
+@pytest.mark.skipif(not O.reference_available(), reason="reference not built here")
+def test_live_reference_bitwise_random_case():
+    p = cube_problem(3, jitter=0.2, seed=99)
+    dt = 0.5 * critical_time_step(p)
+    a = O.run_port(p, 17 * dt, 17, 5)
+    b = O.run_ref(p, 17 * dt, 17, 5)
+    for k in ("u", "v", "a", "f_int", "mass", "F", "sigma"):
+        assert np.array_equal(a[k], b[k]), k

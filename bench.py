@@ -1,0 +1,319 @@
+#!/usr/bin/env python3
+"""Benchmark: hex8 integration-point stress updates per second of the
+explicit neo-Hookean step on a jittered 128^3 cube (2,097,152 elements,
+2,146,689 nodes, 8 Gauss points per element), FP64 plain form.
+
+A step is one central-difference step of the whole mesh: element kernel
+(gather, F, stress, B^T sigma) plus node kernel (assembly gather, a = f/m,
+velocity/displacement update, boundary conditions).  value = 8 E K / device
+time of K steps, with the state resident in HBM.  The FP32-mixed form is
+measured on the same mesh and reported under "variants" with its error
+against the FP64 form.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the CPU implementation of the same step on this
+machine's host cores (the oracle's C restatement of the reference; see
+oracle/), the only place besides the cpu_baseline leg where bench.py runs it.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import signal
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from nimblesm_gb300.mesh import cube_problem, critical_time_step  # noqa: E402
+
+PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
+FALLBACK_HBM_GBS = 6800.0
+METRIC = "hex8 IP stress updates/sec, plain FP64 vs mixed/MLP at <=1e-3 rel. disp error"
+UNIT = "IP-updates/s"
+SCHEDULE_STEPS = 2000  # the workload's schedule: dt = 0.5 dt_crit, 2000 steps
+
+
+def algorithmic_bytes(N, E, precision):
+    """Bytes each step must move once (the ModelData contract after every
+    step): nodes read X, u, v, a, m and write u, v, a, f_int (200 B/node);
+    elements read connectivity and write F and sigma per integration point
+    (992 B/element in FP64, 512 B in FP32).  The element kernel's share is
+    connectivity, F, sigma and the gathered X and u (48 B/node)."""
+    ip = 8 * (9 + 6) * (8 if precision == "fp64" else 4)
+    step = 200 * N + (32 + ip) * E
+    element = (32 + ip) * E + 48 * N
+    return step, element
+
+
+def hbm_peak():
+    try:
+        with open(PEAKS_FILE) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.path = tempfile.mktemp(suffix=".csv")
+        self.proc = None
+        self.device = device
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.send_signal(signal.SIGTERM)
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        try:
+            rows = [r.split(",") for r in open(self.path).read().strip().splitlines() if r.strip()]
+            os.unlink(self.path)
+        except Exception:
+            return None
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows]
+        mx = float(rows[0][2])
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        reasons = sorted({n for r in rows for n, v in zip(names, r[5:9]) if v.strip() == "Active"})
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": reasons, "samples": len(rows)}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def cpu_baseline(problem, dt, seconds_budget=15.0, threads=None):
+    """The oracle (C restatement of the reference's host path) on all host
+    cores, from the workload's initial state, on a bounded number of steps."""
+    from oracle import oracle
+
+    oracle.build(ref=False)
+    threads = threads or os.cpu_count()
+    u = np.zeros_like(problem.coords)
+    v = problem.v_init.copy()
+    v[problem.node_sets["nodelist_1"]] = 0.0
+    a = np.zeros_like(u)
+    t1 = oracle.continue_port(problem, u, v, a, 0.0, dt, 1, threads)  # includes first-touch
+    k = int(max(1, min(40, seconds_budget / max(t1, 1e-3))))
+    secs = oracle.continue_port(problem, u, v, a, dt, dt, k, threads)
+    return {"value": 8.0 * problem.num_elem * k / secs, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{k} steps of the same {round(problem.num_elem ** (1 / 3))}^3 mesh from its initial state "
+                      f"({secs:.1f} s)"}
+
+
+def run_reference(args):
+    """--impl reference: the CPU implementation of the step, all host cores."""
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    from oracle import oracle
+
+    oracle.build(ref=False)
+    n = args.n
+    problem = cube_problem(n, jitter=0.2, seed=0)
+    dt = 0.5 * critical_time_step(problem)
+    threads = os.cpu_count()
+    u = np.zeros_like(problem.coords)
+    v = problem.v_init.copy()
+    v[problem.node_sets["nodelist_1"]] = 0.0
+    a = np.zeros_like(u)
+    t = 0.0
+    for _ in range(max(args.warmup, 1) if args.warmup < 3 else 3):
+        oracle.continue_port(problem, u, v, a, t, dt, 1, threads)
+        t += dt
+    est = oracle.continue_port(problem, u, v, a, t, dt, 1, threads)
+    t += dt
+    # each step is one full explicit step of the mesh; the count is capped so
+    # that the run ends within a few minutes
+    steps = int(min(args.steps, max(1, 120.0 / max(est, 1e-3))))
+    secs = oracle.continue_port(problem, u, v, a, t, dt, steps, threads)
+    value = 8.0 * problem.num_elem * steps / secs
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * secs / steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"hex8 neo-Hookean explicit step, jittered {n}^3 cube (config 1)",
+                   "elements": problem.num_elem, "nodes": problem.num_nodes, "steps_requested": args.steps},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{steps} full steps of the {n}^3 mesh"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    from nimblesm_gb300 import engine as E
+
+    ws, rank, local = dist_env()
+    dist = None
+    if ws > 1:
+        import torch
+        import torch.distributed as tdist
+
+        torch.cuda.set_device(local)
+        tdist.init_process_group("nccl")
+        dist = (torch, tdist)
+
+    n = args.n
+    problem = cube_problem(n, jitter=0.2, seed=0)
+    N, E_ = problem.num_nodes, problem.num_elem
+    dt_crit = critical_time_step(problem)
+    dt = 0.5 * dt_crit
+    final_time = SCHEDULE_STEPS * dt
+    sched = max(SCHEDULE_STEPS, args.warmup + 2 * args.steps + 1)
+    final_time = sched * dt
+
+    def barrier():
+        if dist:
+            dist[1].barrier()
+            dist[0].cuda.synchronize()
+
+    def max_over_ranks(x):
+        if not dist:
+            return x
+        t = dist[0].tensor([x], dtype=dist[0].float64, device="cuda")
+        dist[1].all_reduce(t, op=dist[1].ReduceOp.MAX)
+        return float(t.item())
+
+    results = {}
+    for precision in ([args.precision] + ([p for p in ("fp64", "fp32") if p != args.precision]
+                                          if args.variants else [])):
+        m = E.Model(problem, precision=precision, device=local if ws > 1 else 0)
+        m.begin(final_time, sched, sched)
+        m.advance(args.warmup)
+        m.synchronize()
+        barrier()
+        with ClockSampler(local) as clk:
+            ms = m.advance_timed(args.steps)
+        barrier()
+        ms = max_over_ranks(ms)
+        # per-kernel device times over the same number of steps (events on the
+        # engine's stream around every element and node launch)
+        m.set_profiling(True)
+        m.advance(args.steps)
+        prof = m.get_profile()
+        m.set_profiling(False)
+        state_u = m.GetVectorNodeData("displacement")
+        results[precision] = dict(ms=ms, prof=prof, clocks=clk.summary(), launches=m.launches_per_advance(args.steps),
+                                  u=state_u, model=m)
+        if precision != args.precision:
+            m.close()
+
+    head = results[args.precision]
+    m = head["model"]
+    ms = head["ms"]
+    value = 8.0 * E_ * args.steps * ws / (ms * 1e-3)
+
+    # end to end through the drop-in host-buffer entry point: each step copies
+    # the displacement in from pinned host memory and the internal force out
+    e2e_steps = max(3, min(args.steps, 30))
+    u_host = E.PinnedArray((N, 3))
+    f_host = E.PinnedArray((N, 3))
+    u_host.array[:] = head["u"]
+    m.ComputeInternalForceHost(u_host.array, f_host.array)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        m.ComputeInternalForceHost(u_host.array, f_host.array)
+    t1 = time.perf_counter()
+    barrier()
+    e2e_s = max_over_ranks(t1 - t0)
+    e2e_value = 8.0 * E_ * e2e_steps * ws / e2e_s
+
+    step_bytes, elem_bytes = algorithmic_bytes(N, E_, args.precision)
+    peak, peak_kind = hbm_peak()
+    elem_ms = head["prof"]["element_ms"] / max(head["prof"]["element_launches"], 1)
+    node_ms = head["prof"]["node_ms"] / max(head["prof"]["node_launches"], 1)
+    achieved = elem_bytes / (elem_ms * 1e-3) / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+        "data": "synthetic",
+        "config": {"workload": f"hex8 neo-Hookean explicit step, jittered {n}^3 cube (config 1), "
+                               f"{args.precision}", "elements": E_, "nodes": N, "ips_per_step": 8 * E_,
+                   "dt": dt, "schedule_steps": sched, "parallelism": f"replicas{ws}",
+                   "l2": "inputs larger than L2 (per-step traffic >> 129 MB)"},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 24 * N, "d2h_bytes_per_step": 24 * N,
+                "path": "nsm_compute_internal_force_host (pinned u in, f_int out)", "steps": e2e_steps},
+        "gpu_launches": head["launches"],
+        "roofline": {"bound": "hbm", "kernel": "k_element", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
+                     "algorithmic_bytes_per_launch": elem_bytes, "launch_ms": elem_ms, "node_launch_ms": node_ms,
+                     "step_algorithmic_bytes": step_bytes},
+        "clocks": head["clocks"],
+    }
+    variants = {}
+    for prec, r in results.items():
+        if prec == args.precision:
+            continue
+        v = 8.0 * E_ * args.steps * ws / (r["ms"] * 1e-3)
+        err = float(np.linalg.norm(r["u"] - head["u"]) / max(np.linalg.norm(head["u"]), 1e-300))
+        variants[prec] = {"value": v, "ms_per_step": r["ms"] / args.steps, "speedup_vs_fp64": v / value,
+                          "rel_disp_err_vs_fp64": err, "after_steps": args.warmup + args.steps,
+                          "element_launch_ms": r["prof"]["element_ms"] / max(r["prof"]["element_launches"], 1),
+                          "clocks": r["clocks"]}
+    if variants:
+        line["variants"] = variants
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(problem, dt)
+    m.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist[1].destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--n", type=int, default=128, help="cube divisions (default 128: config 1)")
+    ap.add_argument("--precision", choices=("fp64", "fp32"), default="fp64")
+    ap.add_argument("--no-variants", dest="variants", action="store_false")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

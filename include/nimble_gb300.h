@@ -1,0 +1,188 @@
+/* nimble_gb300 -- C ABI of the GB300 explicit-dynamics engine.
+ *
+ * The engine runs NimbleSM's explicit transient-dynamics step on one GPU:
+ * 8-node hex elements with 2x2x2 Gauss points, neo-Hookean material, lumped
+ * mass, central-difference time integration and velocity / displacement
+ * boundary conditions.  These entry points are what a NimbleSM
+ * ModelDataBase implementation (a "GpuModelData") forwards to: each one names
+ * the reference interface it replaces (paths inside the NimbleSM source tree).
+ *
+ * Conventions
+ *   - Plain C: opaque handles, host pointers and sizes, int status (0 = ok).
+ *     On failure nsm_last_error() describes the error of the calling thread.
+ *   - Host arrays use the reference layouts: node vectors [N][3] (x,y,z per
+ *     node, src/nimble_model_data.cc:540-546), connectivity [E][8] 0-based in
+ *     the reference corner order (src/nimble_element.cc:113-120), integration
+ *     point tensors [E][8][9] full (K_F_* order xx,yy,zz,xy,yz,zx,yx,zy,xz)
+ *     and [E][8][6] symmetric (K_S_* order xx,yy,zz,xy,yz,zx)
+ *     (src/nimble_utils.h:91-109).
+ *   - One handle = one block of elements on one GPU, one CUDA stream.  Calls on
+ *     one handle must not overlap (like the reference's ModelData, which is not
+ *     thread-safe); different handles are independent.
+ *   - Arithmetic: NSM_PRECISION_FP64 computes in IEEE FP64 throughout.
+ *     NSM_PRECISION_FP32_MIXED computes the element work (gradient, F, stress,
+ *     B^T sigma) in FP32 and keeps the nodal state, mass, time step and
+ *     energies in FP64.
+ */
+#ifndef NIMBLE_GB300_H
+#define NIMBLE_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NSM_ABI_VERSION 1
+
+/* Status codes. */
+#define NSM_OK 0
+#define NSM_ERR_INVALID_ARGUMENT 1
+#define NSM_ERR_CUDA 2
+#define NSM_ERR_BAD_JACOBIAN 3   /* an element inverted (det <= 0): the reference asserts, src/nimble_utils.h:1243-1255 */
+#define NSM_ERR_NONFINITE 4      /* NaN/Inf in forces */
+#define NSM_ERR_STATE 5          /* call out of order (e.g. advance before begin) */
+#define NSM_ERR_OUT_OF_MEMORY 6
+
+/* Precision forms. */
+#define NSM_PRECISION_FP64 0
+#define NSM_PRECISION_FP32_MIXED 1
+
+/* Node fields (ModelData field labels, src/nimble_data_manager.cc:135-156). */
+#define NSM_FIELD_REFERENCE_COORDINATE 0
+#define NSM_FIELD_DISPLACEMENT 1
+#define NSM_FIELD_VELOCITY 2
+#define NSM_FIELD_ACCELERATION 3
+#define NSM_FIELD_INTERNAL_FORCE 4
+#define NSM_FIELD_EXTERNAL_FORCE 5
+
+/* Boundary-condition kinds (BoundaryCondition::BC_TYPE,
+ * src/nimble_boundary_condition.h; parsed at src/nimble_boundary_condition.cc:65-144). */
+#define NSM_BC_INITIAL_VELOCITY 0
+#define NSM_BC_PRESCRIBED_VELOCITY 1
+#define NSM_BC_PRESCRIBED_DISPLACEMENT 2
+
+typedef struct nsm_model nsm_model;
+
+typedef struct nsm_mesh_desc {
+  int           num_nodes;
+  int           num_elem;
+  const double* coords; /* [N][3] reference coordinates */
+  const int*    conn;   /* [E][8] */
+} nsm_mesh_desc;
+
+/* "neohookean density .. bulk_modulus .. shear_modulus .."
+ * (NeohookeanMaterial, src/nimble_material.cc:208-224). */
+typedef struct nsm_neohookean {
+  double density;
+  double bulk_modulus;
+  double shear_modulus;
+} nsm_neohookean;
+
+typedef struct nsm_options {
+  int precision;     /* NSM_PRECISION_* */
+  int store_ip_data; /* 1: write F and sigma per integration point every step (the
+                        ModelData element-data contract); 0: only on output steps */
+  int device;        /* CUDA device ordinal */
+  int graph_steps;   /* steps per captured CUDA graph in nsm_advance (0 = default 50) */
+} nsm_options;
+
+const char* nsm_last_error(void);
+int         nsm_abi_version(void);
+
+/* Mesh upload and one-time setup: reference geometry per integration point,
+ * lumped mass and critical time step.  Replaces DataManager construction
+ * (src/nimble_data_manager.cc:69-159) plus ModelData::InitializeBlocks
+ * (src/nimble_model_data.cc:484-493) for one block. */
+int nsm_create(const nsm_mesh_desc* mesh, const nsm_neohookean* material, const nsm_options* options,
+               nsm_model** out);
+int nsm_destroy(nsm_model* model);
+
+/* One boundary-condition line "<kind> <nodeset> <x|y|z> <value>" over a node
+ * list, in deck order (BoundaryConditionManager::Initialize,
+ * src/nimble_boundary_condition_manager.cc:52-72).  component 0..2. */
+int nsm_add_boundary_condition(nsm_model* model, int kind, int component, double value, const int* nodes,
+                               int num_nodes);
+
+/* ModelData::ComputeLumpedMass (src/nimble_model_data.cc:495-530): the mass is
+ * computed at nsm_create; this copies it out ([N], nullable). */
+int nsm_compute_lumped_mass(nsm_model* model, double* lumped_mass);
+/* ModelDataBase::GetCriticalTimeStep (src/nimble_model_data_base.h:297-300,
+ * computed by src/nimble_block_base.cc:51-84). */
+int nsm_critical_time_step(nsm_model* model, double* dt);
+
+/* ModelDataBase::ApplyInitialConditions / ApplyKinematicConditions
+ * (src/nimble_model_data_base.cc:83-100). */
+int nsm_apply_initial_conditions(nsm_model* model);
+int nsm_apply_kinematic_conditions(nsm_model* model, double time_current, double time_previous);
+
+/* GetVectorNodeData views (src/nimble_model_data_base.h) as copies to / from
+ * host [N][3] arrays. */
+int nsm_set_node_field(nsm_model* model, int field, const double* values);
+int nsm_get_node_field(nsm_model* model, int field, double* values);
+
+/* ModelData::ComputeInternalForce (src/nimble_model_data.cc:620-667 ->
+ * Block::ComputeInternalForce, src/nimble_block.cc:388-436) from the device
+ * displacement into the device internal force; F_np1 and sigma_np1 are kept
+ * per integration point. */
+int nsm_compute_internal_force(nsm_model* model, double time_previous, double time_current, int is_output_step);
+
+/* The same, with the displacement and the force in host memory: what the
+ * reference's integrator loop (which updates nodes on the host) calls each
+ * step through a GpuModelData.  displacement, internal_force: [N][3]. */
+int nsm_compute_internal_force_host(nsm_model* model, const double* displacement, double* internal_force);
+
+/* Element data of the last internal-force evaluation, reference layout
+ * (ModelData element data n/np1, src/nimble_model_data.cc:142-169).
+ * F: [E][8][9], sigma: [E][8][6]; either may be NULL. */
+int nsm_get_ip_data(nsm_model* model, double* F, double* sigma);
+
+/* Kinetic energy 1/2 sum m v.v and internal energy sum det(J_X) W(F) over the
+ * integration points (not in the reference; used for energy balance). */
+int nsm_get_energies(nsm_model* model, double* kinetic, double* internal);
+
+/* The explicit loop of ExplicitTimeIntegrator::Integrate
+ * (src/integrators/explicit_time_integrator.cc:123-278), on the device:
+ * nsm_begin fixes the schedule (dt = (final - initial) / num_steps, output
+ * steps every output_frequency and at the last step, 0 = none), zeroes the
+ * state, applies the initial conditions, writes the optional initial velocity
+ * v_init ([N][3], after ApplyInitialConditions) and applies the kinematic
+ * conditions at t = 0.  nsm_advance runs the next num_steps steps of the
+ * schedule as captured CUDA graphs; the state after each call is the
+ * reference's state after that many steps. */
+int nsm_begin(nsm_model* model, double initial_time, double final_time, int num_steps, int output_frequency,
+              const double* v_init);
+int nsm_advance(nsm_model* model, int num_steps);
+/* nsm_advance bracketed by CUDA events on the handle's stream; waits for the
+ * steps and returns their device time in milliseconds. */
+int nsm_advance_timed(nsm_model* model, int num_steps, double* device_ms);
+/* Steps done since nsm_begin and the current time. */
+int nsm_progress(nsm_model* model, int* steps_done, double* time_current);
+int nsm_synchronize(nsm_model* model);
+
+/* Device status word accumulated since the last call (NSM_ERR_* mapped from
+ * kernel-side checks: inverted elements, non-finite forces); clears it. */
+int nsm_check_status(nsm_model* model);
+
+/* Timing helpers for measurement: mean device time (CUDA events on the
+ * handle's stream) of `repeats` launches of the element kernel alone and of
+ * the node kernel alone, in milliseconds. */
+int nsm_time_kernels(nsm_model* model, int repeats, double* element_ms, double* node_ms);
+/* Number of kernel launches nsm_advance(model, num_steps) issues. */
+int nsm_launches_per_advance(nsm_model* model, int num_steps);
+/* Profiling mode: nsm_advance launches without CUDA graphs and brackets each
+ * element and node kernel with CUDA events on the handle's stream;
+ * nsm_get_profile returns (and resets) the summed device times and counts. */
+int nsm_set_profiling(nsm_model* model, int enable);
+int nsm_get_profile(nsm_model* model, double* element_ms_total, int* element_launches, double* node_ms_total,
+                    int* node_launches);
+
+/* Pinned host memory for the host-buffer entry points (page-locked so that the
+ * copies run at full link bandwidth). */
+void* nsm_host_alloc(size_t bytes);
+void  nsm_host_free(void* ptr);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,298 @@
+// Fused hex8 element kernel: gather -> deformation gradient -> neo-Hookean
+// Cauchy stress -> B^T sigma, one thread per element, for the FP64 plain form
+// and the FP32 mixed form (same code, T = double / float).  The element math
+// and the reasons for its form are in hex_math.cuh.
+#include "hex_math.cuh"
+#include "nsm_kernels.cuh"
+
+namespace nsm {
+
+// FP64 form: reference geometry precomputed (geo planes).  FP32 form: the
+// reference Jacobian is rebuilt from X each step with the same transform.
+template <typename T, bool kPrecomputedGeo>
+__global__ void __launch_bounds__(128) k_element(ElementArgs a)
+{
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= a.E) return;
+  const long ld_e = a.ld_e, ld_n = a.ld_n;
+
+  int id[8];
+#pragma unroll
+  for (int n = 0; n < 8; n++) id[n] = __ldg(&a.conn[n * ld_e + e]);
+
+  // displacement gradient at the points (36 distinct values)
+  T Gu[3][3][2][2];
+  {
+    T x[8][3];
+#pragma unroll
+    for (int n = 0; n < 8; n++)
+#pragma unroll
+      for (int k = 0; k < 3; k++) x[n][k] = T(__ldg(&a.u[k * ld_n + id[n]]));
+    nodal_gradient<T>(x, Gu);
+  }
+  T GX[3][3][2][2];
+  if (!kPrecomputedGeo) {
+    T x[8][3];
+#pragma unroll
+    for (int n = 0; n < 8; n++)
+#pragma unroll
+      for (int k = 0; k < 3; k++) x[n][k] = T(__ldg(&a.X[k * ld_n + id[n]]));
+    nodal_gradient<T>(x, GX);
+  }
+
+  T S[3][3][2][2];  // point sums of Q[d][i] grouped by the other-axis sign pairs
+#pragma unroll
+  for (int d = 0; d < 3; d++)
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int s = 0; s < 2; s++)
+#pragma unroll
+        for (int t = 0; t < 2; t++) S[d][i][s][t] = T(0);
+
+  const T K = T(a.bulk), Gm = T(a.shear);
+  bool    bad = false;
+  T*      Fo  = reinterpret_cast<T*>(a.F);
+  T*      So  = reinterpret_cast<T*>(a.sigma);
+  const bool store = a.store_ip || (a.sched != nullptr && a.sched[*a.step_base + a.k].is_output);
+
+#pragma unroll
+  for (int p = 0; p < 8; p++) {
+    const int bit[3] = {sx_of(p), sy_of(p), sz_of(p)};
+    T         G0[3][3], det0;
+    if (kPrecomputedGeo) {
+#pragma unroll
+      for (int q = 0; q < 9; q++) G0[q / 3][q % 3] = T(__ldg(&a.geo[(p * 10 + q) * ld_e + e]));
+      det0 = T(__ldg(&a.geo[(p * 10 + 9) * ld_e + e]));
+    } else {
+      T JX[3][3];
+#pragma unroll
+      for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int d = 0; d < 3; d++) JX[i][d] = GX[d][i][bit[other1(d)]][bit[other2(d)]];
+      invert3<T>(JX, G0, det0);
+    }
+    // H[i][J] = sum_d du_i/dxi_d G0[d][J]
+    T H[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int J = 0; J < 3; J++) {
+        T h = T(0);
+#pragma unroll
+        for (int d = 0; d < 3; d++) h += Gu[d][i][bit[other1(d)]][bit[other2(d)]] * G0[d][J];
+        H[i][J] = h;
+      }
+    T sig[6], C[3][3], J;
+    neohookean<T>(H, K, Gm, sig, C, J);
+    if (!(J > T(0)) || !(det0 > T(0))) bad = true;  // inverted element
+    if (store) {
+#pragma unroll
+      for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int k = 0; k < 3; k++) Fo[(p * 9 + full_slot(i, k)) * ld_e + e] = (i == k) ? T(1) + H[i][k] : H[i][k];
+#pragma unroll
+      for (int q = 0; q < 6; q++) So[(p * 6 + q) * ld_e + e] = sig[q];
+    }
+    // P = sigma cof(F);  Q[d][i] = det J_X sum_J G0[d][J] P[i][J]
+    T P[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int J = 0; J < 3; J++)
+        P[i][J] = sym(sig, i, 0) * C[0][J] + sym(sig, i, 1) * C[1][J] + sym(sig, i, 2) * C[2][J];
+#pragma unroll
+    for (int d = 0; d < 3; d++)
+#pragma unroll
+      for (int i = 0; i < 3; i++) {
+        T q = G0[d][0] * P[i][0] + G0[d][1] * P[i][1] + G0[d][2] * P[i][2];
+        S[d][i][bit[other1(d)]][bit[other2(d)]] += det0 * q;
+      }
+  }
+
+  // f_a,i = - sum_p sum_d dN_a/dxi_d(p) Q_p[d][i]
+  T f[8][3];
+#pragma unroll
+  for (int n = 0; n < 8; n++)
+#pragma unroll
+    for (int i = 0; i < 3; i++) f[n][i] = T(0);
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    const int o1 = other1(d), o2 = other2(d);
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      T R[2][2];
+      bwd_transform<T>(S[d][i], R);
+#pragma unroll
+      for (int b = 0; b < 2; b++)
+#pragma unroll
+        for (int c = 0; c < 2; c++) {
+          f[corner_axes(d, 1, o1, b, o2, c)][i] -= R[b][c];
+          f[corner_axes(d, 0, o1, b, o2, c)][i] += R[b][c];
+        }
+    }
+  }
+  T*   fo     = reinterpret_cast<T*>(a.fe);
+  bool finite = true;
+#pragma unroll
+  for (int n = 0; n < 8; n++)
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      fo[(n * 3 + i) * ld_e + e] = f[n][i];
+      finite = finite && isfinite(f[n][i]);
+    }
+  if (bad || !finite) atomicOr(a.status, (bad ? NSM_STATUS_BAD_JACOBIAN : 0) | (finite ? 0 : NSM_STATUS_NONFINITE));
+}
+
+cudaError_t launch_element_fp64(const ElementArgs& a, cudaStream_t stream)
+{
+  if (a.E == 0) return cudaSuccess;
+  k_element<double, true><<<grid_for(a.E, 128), 128, 0, stream>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_element_fp32(const ElementArgs& a, cudaStream_t stream)
+{
+  if (a.E == 0) return cudaSuccess;
+  k_element<float, false><<<grid_for(a.E, 128), 128, 0, stream>>>(a);
+  return cudaGetLastError();
+}
+
+// Energies of the current state, FP64 whatever the element precision:
+// kinetic 1/2 m v.v per node and internal det J_X W(F) per point, with H
+// rebuilt from u (so an FP32 F store does not limit the energy's accuracy).
+// Per-block partial sums in a fixed order, then one block: deterministic.
+__global__ void __launch_bounds__(128) k_energy_partials(int N, long ld_n, const double* __restrict__ mass,
+                                                         const double* __restrict__ v, int E, long ld_e,
+                                                         const int* __restrict__ conn, const double* __restrict__ u,
+                                                         const double* __restrict__ geo, double K, double Gm,
+                                                         double* __restrict__ partial)
+{
+  __shared__ double s_ke[128], s_ie[128];
+  double            ke = 0.0, ie = 0.0;
+  for (long n = blockIdx.x * (long)blockDim.x + threadIdx.x; n < N; n += (long)gridDim.x * blockDim.x) {
+    double vx = v[n], vy = v[ld_n + n], vz = v[2 * ld_n + n];
+    ke += 0.5 * mass[n] * (vx * vx + vy * vy + vz * vz);
+  }
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < E; e += (long)gridDim.x * blockDim.x) {
+    double x[8][3];
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+      int id = conn[c * ld_e + e];
+#pragma unroll
+      for (int k = 0; k < 3; k++) x[c][k] = u[k * ld_n + id];
+    }
+    double Gu[3][3][2][2];
+    nodal_gradient<double>(x, Gu);
+#pragma unroll 1
+    for (int p = 0; p < 8; p++) {
+      const int bit[3] = {sx_of(p), sy_of(p), sz_of(p)};
+      double    G0[3][3];
+      for (int q = 0; q < 9; q++) G0[q / 3][q % 3] = geo[(p * 10 + q) * ld_e + e];
+      double H[3][3];
+      for (int i = 0; i < 3; i++)
+        for (int J = 0; J < 3; J++) {
+          double h = 0.0;
+          for (int d = 0; d < 3; d++) {
+            const int o1 = other1(d), o2 = other2(d);
+            h += Gu[d][i][bit[o1]][bit[o2]] * G0[d][J];
+          }
+          H[i][J] = h;
+        }
+      ie += geo[(p * 10 + 9) * ld_e + e] * energy_density(H, K, Gm);
+    }
+  }
+  s_ke[threadIdx.x] = ke;
+  s_ie[threadIdx.x] = ie;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) {
+      s_ke[threadIdx.x] += s_ke[threadIdx.x + w];
+      s_ie[threadIdx.x] += s_ie[threadIdx.x + w];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    partial[2 * blockIdx.x]     = s_ke[0];
+    partial[2 * blockIdx.x + 1] = s_ie[0];
+  }
+}
+
+__global__ void k_energy_final(int nblocks, const double* __restrict__ partial, double* __restrict__ out)
+{
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double ke = 0.0, ie = 0.0;
+  for (int b = 0; b < nblocks; b++) {
+    ke += partial[2 * b];
+    ie += partial[2 * b + 1];
+  }
+  out[0] = ke;
+  out[1] = ie;
+}
+
+cudaError_t launch_energies(int N, long ld_n, const double* mass, const double* v, int E, long ld_e,
+                            const int* conn, const double* u, const double* geo, double bulk, double shear,
+                            double* partial, double* out, cudaStream_t stream)
+{
+  const int blocks = kEnergyBlocks;
+  k_energy_partials<<<blocks, 128, 0, stream>>>(N, ld_n, mass, v, E, ld_e, conn, u, geo, bulk, shear, partial);
+  k_energy_final<<<1, 32, 0, stream>>>(blocks, partial, out);
+  return cudaGetLastError();
+}
+
+// SoA integration-point planes src[(p*comps + c)*ld_e + e] -> reference
+// layout dst[(e*8 + p)*comps + c] (doubles).
+template <typename T>
+__global__ void k_ip_to_aos(int E, long ld_e, const T* __restrict__ src, int comps, double* __restrict__ dst)
+{
+  long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  long total = (long)E * 8 * comps;
+  if (i >= total) return;
+  int  c = (int)(i % comps);
+  long r = i / comps;
+  int  p = (int)(r % 8);
+  long e = r / 8;
+  dst[i] = (double)src[(p * comps + c) * ld_e + e];
+}
+
+cudaError_t launch_ip_to_aos(int E, long ld_e, const void* src, int src_is_float, int comps, double* dst,
+                             cudaStream_t stream)
+{
+  long total = (long)E * 8 * comps;
+  if (total == 0) return cudaSuccess;
+  if (src_is_float)
+    k_ip_to_aos<float><<<grid_for(total, 256), 256, 0, stream>>>(E, ld_e, (const float*)src, comps, dst);
+  else
+    k_ip_to_aos<double><<<grid_for(total, 256), 256, 0, stream>>>(E, ld_e, (const double*)src, comps, dst);
+  return cudaGetLastError();
+}
+
+__global__ void k_node_soa_to_aos(int N, long ld_n, const double* __restrict__ src, double* __restrict__ dst)
+{
+  long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= 3L * N) return;
+  dst[i] = src[(i % 3) * ld_n + i / 3];
+}
+
+__global__ void k_node_aos_to_soa(int N, long ld_n, const double* __restrict__ src, double* __restrict__ dst)
+{
+  long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= 3L * N) return;
+  dst[(i % 3) * ld_n + i / 3] = src[i];
+}
+
+cudaError_t launch_node_soa_to_aos(int N, long ld_n, const double* src, double* dst, cudaStream_t stream)
+{
+  if (N == 0) return cudaSuccess;
+  k_node_soa_to_aos<<<grid_for(3L * N, 256), 256, 0, stream>>>(N, ld_n, src, dst);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_node_aos_to_soa(int N, long ld_n, const double* src, double* dst, cudaStream_t stream)
+{
+  if (N == 0) return cudaSuccess;
+  k_node_aos_to_soa<<<grid_for(3L * N, 256), 256, 0, stream>>>(N, ld_n, src, dst);
+  return cudaGetLastError();
+}
+
+}  // namespace nsm

@@ -1,0 +1,132 @@
+// Node kernels: assembly of the element forces and the central-difference
+// update.  Compiled with --fmad=false: every product and sum rounds exactly
+// as the reference's host loops do, so given the same element forces the
+// nodal state equals the reference's bit for bit.
+#include "nsm_kernels.cuh"
+
+namespace nsm {
+
+// ApplyKinematicBC for the explicit scheme, constant magnitudes
+// (src/nimble_boundary_condition_manager.h:136-217): prescribed velocity sets
+// v; prescribed displacement sets v = (d - u) / delta when delta > 0.
+__device__ __forceinline__ void apply_bc(const NodeBC& bc, double delta, const double u[3], double v[3])
+{
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    if (bc.kind[k] == 1) {
+      v[k] = bc.value[k];
+    } else if (bc.kind[k] == 2 && delta > 0.0) {
+      v[k] = (bc.value[k] - u[k]) / delta;
+    }
+  }
+}
+
+template <typename TF>
+__global__ void __launch_bounds__(256) k_node_update(NodeArgs a)
+{
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= a.N) return;
+  const long ld = a.ld_n;
+  double     u[3], v[3], acc[3];
+  const int  slot = a.bc_slot[n];
+  NodeBC     bc;
+  if (slot >= 0) bc = a.bcs[slot];
+
+  if (a.k_post >= 0 || a.gather_only) {
+    // ModelData::ComputeInternalForce: zero, then element contributions in
+    // increasing element order (src/nimble_model_data.cc:620-667,
+    // src/nimble_block.cc:373-383).
+    const TF* fe = reinterpret_cast<const TF*>(a.fe);
+    double    f[3] = {0.0, 0.0, 0.0};
+    for (int k = a.node_ptr[n]; k < a.node_ptr[n + 1]; k++) {
+      const int  ec = __ldg(&a.node_inc[k]);
+      const long e  = ec >> 3;
+      const int  c  = ec & 7;
+#pragma unroll
+      for (int i = 0; i < 3; i++) f[i] += (double)__ldg(&fe[(c * 3 + i) * a.ld_e + e]);
+    }
+#pragma unroll
+    for (int i = 0; i < 3; i++) a.f_int[i * ld + n] = f[i];
+    if (a.gather_only) return;
+    const StepSched s  = a.sched[*a.step_base + a.k_post];
+    const double    im = a.inv_mass[n];
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      // a = (1/m) (f_int + f_ext), f_ext = 0 (src/integrators/explicit_time_integrator.cc:250-257)
+      acc[i] = im * (f[i] + 0.0);
+      v[i]   = a.v[i * ld + n] + s.half * acc[i];
+      u[i]   = a.u[i * ld + n];
+    }
+    if (s.is_output && slot >= 0) apply_bc(bc, s.delta, u, v);
+  } else {
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      acc[i] = a.a[i * ld + n];
+      v[i]   = a.v[i * ld + n];
+      u[i]   = a.u[i * ld + n];
+    }
+  }
+  if (a.k_pre >= 0) {
+    // v^{n+1/2} = v^n + dt/2 a^n; BCs; u^{n+1} = u^n + dt v^{n+1/2}; BCs
+    // (src/integrators/explicit_time_integrator.cc:200-223)
+    const StepSched s = a.sched[*a.step_base + a.k_pre];
+#pragma unroll
+    for (int i = 0; i < 3; i++) v[i] = v[i] + s.half * acc[i];
+    if (slot >= 0) apply_bc(bc, s.delta, u, v);
+#pragma unroll
+    for (int i = 0; i < 3; i++) u[i] = u[i] + s.delta * v[i];
+    if (slot >= 0) apply_bc(bc, s.delta, u, v);
+  }
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    a.u[i * ld + n] = u[i];
+    a.v[i * ld + n] = v[i];
+    if (a.k_post >= 0) a.a[i * ld + n] = acc[i];
+  }
+}
+
+cudaError_t launch_node_update(const NodeArgs& a, cudaStream_t stream)
+{
+  if (a.N == 0) return cudaSuccess;
+  if (a.fe_is_float)
+    k_node_update<float><<<grid_for(a.N, 256), 256, 0, stream>>>(a);
+  else
+    k_node_update<double><<<grid_for(a.N, 256), 256, 0, stream>>>(a);
+  return cudaGetLastError();
+}
+
+__global__ void k_advance_base(int* base, int k) { *base += k; }
+
+cudaError_t launch_advance_base(int* step_base, int k, cudaStream_t stream)
+{
+  k_advance_base<<<1, 1, 0, stream>>>(step_base, k);
+  return cudaGetLastError();
+}
+
+__global__ void k_apply_bc(int N, long ld_n, const int* __restrict__ bc_slot, const NodeBC* __restrict__ bcs,
+                           double delta, const double* __restrict__ u, double* __restrict__ v)
+{
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  const int slot = bc_slot[n];
+  if (slot < 0) return;
+  double uu[3], vv[3];
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    uu[i] = u[i * ld_n + n];
+    vv[i] = v[i * ld_n + n];
+  }
+  apply_bc(bcs[slot], delta, uu, vv);
+#pragma unroll
+  for (int i = 0; i < 3; i++) v[i * ld_n + n] = vv[i];
+}
+
+cudaError_t launch_apply_bc(int N, long ld_n, const int* bc_slot, const NodeBC* bcs, double delta, const double* u,
+                            double* v, cudaStream_t stream)
+{
+  if (N == 0) return cudaSuccess;
+  k_apply_bc<<<grid_for(N, 256), 256, 0, stream>>>(N, ld_n, bc_slot, bcs, delta, u, v);
+  return cudaGetLastError();
+}
+
+}  // namespace nsm

@@ -1,0 +1,103 @@
+// Kernel launch interfaces of the engine (device layouts are structure of
+// arrays: a node field of 3 components is three planes of ld_n doubles; an
+// element field is planes of ld_e entries, one plane per component).
+#pragma once
+
+#include "nsm_common.cuh"
+
+// Device status word bits (read back by the host, returned as C status codes).
+#define NSM_STATUS_BAD_JACOBIAN 1   // a non-positive Jacobian determinant (inverted element)
+#define NSM_STATUS_NONFINITE 2      // a NaN or Inf in a stress or force
+#define NSM_STATUS_MLP_FALLBACK 4   // points left the learned closure's envelope (informational)
+
+namespace nsm {
+
+struct SetupArgs {
+  int           N, E;
+  long          ld_n, ld_e;
+  const int*    conn;      // [8][ld_e]
+  const double* X;         // [3][ld_n]
+  const int*    node_ptr;  // [N+1]
+  const int*    node_inc;  // 8*e + corner, increasing e per node
+  double        density, sound_speed;
+  double*       geo;       // [80][ld_e]
+  double*       me;        // [8][ld_e]
+  double*       dt_elem;   // [E]
+  double*       dt_partial;// [1024]
+  double*       dt_out;    // [1]
+  double*       mass;      // [N]
+  double*       inv_mass;  // [N]
+  int*          status;
+};
+
+void        shape_tables(double* N, double* dN);
+cudaError_t upload_shape_tables(cudaStream_t stream);
+cudaError_t launch_setup(const SetupArgs& a, cudaStream_t stream);
+
+// Element kernel arguments (one launch = all elements of a block).
+struct ElementArgs {
+  int           E;
+  long          ld_e, ld_n;
+  const int*    conn;      // [8][ld_e]
+  const double* u;         // [3][ld_n] displacement
+  const double* X;         // [3][ld_n] reference coordinates (FP32 form only)
+  const double* geo;       // [80][ld_e] G0 and det J0 per ip (FP64 form only)
+  double        bulk, shear;
+  void*         F;         // [72][ld_e] deformation gradient per ip, reference slot order (T)
+  void*         sigma;     // [48][ld_e] Cauchy stress per ip (T)
+  void*         fe;        // [24][ld_e] element nodal forces, corner-major (T)
+  int               store_ip;   // 1: write F and sigma; 0: only on output steps of the schedule
+  const StepSched*  sched;      // schedule (nullable: outside the time loop)
+  const int*        step_base;  // device step counter
+  int               k;          // schedule offset of this step
+  int*              status;
+};
+
+cudaError_t launch_element_fp64(const ElementArgs& a, cudaStream_t stream);
+cudaError_t launch_element_fp32(const ElementArgs& a, cudaStream_t stream);
+
+// Node kernel: the end of step s (gather f_int, a = f/m, v += half*a, output
+// BCs) fused with the start of step s+1 (v += half*a, BCs, u += delta*v, BCs).
+struct NodeArgs {
+  int               N;
+  long              ld_n, ld_e;
+  const int*        node_ptr;
+  const int*        node_inc;
+  const void*       fe;       // element nodal forces (double or float)
+  int               fe_is_float;
+  const double*     inv_mass;
+  const int*        bc_slot;  // [N] -1 or index into bcs
+  const NodeBC*     bcs;
+  const StepSched*  sched;    // per-step schedule
+  const int*        step_base;// device step counter (schedule index of step "k = 0")
+  int               k_post;   // schedule offset of the step being finished, or -1
+  int               k_pre;    // schedule offset of the step being started, or -1
+  int               gather_only; // only f_int = gather(fe); no state update
+  double*           u;
+  double*           v;
+  double*           a;
+  double*           f_int;
+};
+
+cudaError_t launch_node_update(const NodeArgs& a, cudaStream_t stream);
+cudaError_t launch_advance_base(int* step_base, int k, cudaStream_t stream);
+
+// Kinematic conditions alone (ApplyKinematicConditions with delta_t), and
+// initial conditions (velocity values).
+cudaError_t launch_apply_bc(int N, long ld_n, const int* bc_slot, const NodeBC* bcs, double delta, const double* u,
+                            double* v, cudaStream_t stream);
+
+// Energies: kinetic 1/2 m v.v (per-node) and internal sum det J0 W(F) per ip;
+// two-pass deterministic sums into out[0], out[1].
+constexpr int kEnergyBlocks = 608;  // 4 x 152 SMs; partial buffer holds 2 doubles per block
+cudaError_t   launch_energies(int N, long ld_n, const double* mass, const double* v, int E, long ld_e,
+                              const int* conn, const double* u, const double* geo, double bulk, double shear,
+                              double* partial, double* out, cudaStream_t stream);
+
+// Reference-layout views of SoA data ([E][8][9] / [E][8][6] / [N][3]).
+cudaError_t launch_ip_to_aos(int E, long ld_e, const void* src, int src_is_float, int comps, double* dst,
+                             cudaStream_t stream);
+cudaError_t launch_node_soa_to_aos(int N, long ld_n, const double* src, double* dst, cudaStream_t stream);
+cudaError_t launch_node_aos_to_soa(int N, long ld_n, const double* src, double* dst, cudaStream_t stream);
+
+}  // namespace nsm

@@ -1,0 +1,809 @@
+// Host engine of the C ABI (include/nimble_gb300.h): device-resident
+// ModelData for one block, the explicit loop as captured CUDA graphs, and the
+// host-buffer entry points.  C++ host code; all arithmetic on the path runs
+// in the kernels (setup_kernels.cu, element_kernels.cu, node_kernels.cu).
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/nimble_gb300.h"
+#include "nsm_kernels.cuh"
+
+using nsm::NodeBC;
+using nsm::StepSched;
+
+namespace {
+
+thread_local std::string g_error;
+
+int fail(int code, const std::string& msg)
+{
+  g_error = msg;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* where)
+{
+  g_error = std::string(where) + ": " + cudaGetErrorString(e);
+  return e == cudaErrorMemoryAllocation ? NSM_ERR_OUT_OF_MEMORY : NSM_ERR_CUDA;
+}
+
+#define NSM_CUDA(call)                                    \
+  do {                                                    \
+    cudaError_t _e = (call);                              \
+    if (_e != cudaSuccess) return cuda_fail(_e, #call);   \
+  } while (0)
+
+long pad(long n, long q) { return (n + q - 1) / q * q; }
+
+struct BcLine {
+  int              kind, component;
+  double           value;
+  std::vector<int> nodes;
+};
+
+}  // namespace
+
+struct nsm_model {
+  int          N = 0, E = 0;
+  long         ld_n = 0, ld_e = 0;
+  int          precision = NSM_PRECISION_FP64, store_ip = 1, graph_steps = 50, device = 0;
+  double       density = 0, K = 0, G = 0, dt_crit = 0;
+  cudaStream_t stream = nullptr;
+
+  int*    d_conn = nullptr;  // [8][ld_e]
+  int*    d_node_ptr = nullptr;
+  int*    d_node_inc = nullptr;
+  double* d_X = nullptr;  // node planes [3][ld_n]
+  double* d_u = nullptr;
+  double* d_v = nullptr;
+  double* d_a = nullptr;
+  double* d_f = nullptr;
+  double* d_fext = nullptr;
+  double* d_mass = nullptr;
+  double* d_inv_mass = nullptr;
+  double* d_geo = nullptr;  // [80][ld_e]
+  void*   d_F = nullptr;    // [72][ld_e]
+  void*   d_sigma = nullptr;// [48][ld_e]
+  void*   d_fe = nullptr;   // [24][ld_e]
+  int*    d_status = nullptr;
+  int*    d_step_base = nullptr;
+  double* d_scratch = nullptr;  // energy partials / setup temporaries
+  double* d_stage = nullptr;    // [3N] AoS staging for host copies
+  double* d_out = nullptr;      // small results
+
+  std::vector<BcLine> bcs;
+  bool                bcs_dirty = true;
+  int*                d_bc_slot = nullptr;
+  NodeBC*             d_bcs = nullptr;
+  int*                d_ibc_slot = nullptr;
+  NodeBC*             d_ibcs = nullptr;
+
+  // schedule
+  bool                   begun = false;
+  int                    num_steps = 0, steps_done = 0;
+  std::vector<StepSched> h_sched;
+  std::vector<double>    h_time;  // time after each step
+  double                 t0 = 0;
+  StepSched*             d_sched = nullptr;
+
+  std::map<int, cudaGraphExec_t> graphs;
+
+  // profiling
+  bool                                              profiling = false;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_elem, ev_node;
+  size_t                                            ev_elem_used = 0, ev_node_used = 0;
+
+  size_t elem_bytes() const { return precision == NSM_PRECISION_FP64 ? 8 : 4; }
+};
+
+namespace {
+
+void free_all(nsm_model* m)
+{
+  for (auto& g : m->graphs) cudaGraphExecDestroy(g.second);
+  m->graphs.clear();
+  void* ptrs[] = {m->d_conn, m->d_node_ptr, m->d_node_inc, m->d_X,     m->d_u,         m->d_v,     m->d_a,
+                  m->d_f,    m->d_fext,     m->d_mass,     m->d_inv_mass, m->d_geo,    m->d_F,     m->d_sigma,
+                  m->d_fe,   m->d_status,   m->d_step_base, m->d_scratch, m->d_stage,  m->d_out,   m->d_bc_slot,
+                  m->d_bcs,  m->d_ibc_slot, m->d_ibcs,     m->d_sched};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  for (auto& e : m->ev_elem) {
+    cudaEventDestroy(e.first);
+    cudaEventDestroy(e.second);
+  }
+  for (auto& e : m->ev_node) {
+    cudaEventDestroy(e.first);
+    cudaEventDestroy(e.second);
+  }
+  if (m->stream) cudaStreamDestroy(m->stream);
+}
+
+int read_status(nsm_model* m)
+{
+  int status = 0;
+  NSM_CUDA(cudaMemcpyAsync(&status, m->d_status, sizeof(int), cudaMemcpyDeviceToHost, m->stream));
+  NSM_CUDA(cudaMemsetAsync(m->d_status, 0, sizeof(int), m->stream));
+  NSM_CUDA(cudaStreamSynchronize(m->stream));
+  if (status & NSM_STATUS_BAD_JACOBIAN) return fail(NSM_ERR_BAD_JACOBIAN, "non-positive Jacobian (inverted element)");
+  if (status & NSM_STATUS_NONFINITE) return fail(NSM_ERR_NONFINITE, "non-finite element force");
+  return NSM_OK;
+}
+
+// Per-node boundary-condition tables: the last line in deck order wins per
+// (node, component), as each line overwrites the component it names.
+int upload_bcs(nsm_model* m)
+{
+  if (!m->bcs_dirty) return NSM_OK;
+  for (int pass = 0; pass < 2; pass++) {
+    std::vector<int>    slot(m->N, -1);
+    std::vector<NodeBC> table;
+    for (const BcLine& b : m->bcs) {
+      bool initial = b.kind == NSM_BC_INITIAL_VELOCITY;
+      if ((pass == 0) == initial) continue;  // pass 0: kinematic lines, pass 1: initial velocity
+      for (int n : b.nodes) {
+        if (slot[n] < 0) {
+          slot[n] = (int)table.size();
+          NodeBC z;
+          std::memset(&z, 0, sizeof(z));
+          table.push_back(z);
+        }
+        NodeBC& t          = table[slot[n]];
+        t.kind[b.component]  = (int8_t)(initial ? 1 : (b.kind == NSM_BC_PRESCRIBED_VELOCITY ? 1 : 2));
+        t.value[b.component] = b.value;
+      }
+    }
+    int*&    d_slot = pass == 0 ? m->d_bc_slot : m->d_ibc_slot;
+    NodeBC*& d_tab  = pass == 0 ? m->d_bcs : m->d_ibcs;
+    if (d_tab) cudaFree(d_tab);
+    d_tab = nullptr;
+    if (!d_slot) NSM_CUDA(cudaMalloc(&d_slot, sizeof(int) * (size_t)(m->N > 0 ? m->N : 1)));
+    if (!table.empty()) {
+      NSM_CUDA(cudaMalloc(&d_tab, sizeof(NodeBC) * table.size()));
+      NSM_CUDA(cudaMemcpyAsync(d_tab, table.data(), sizeof(NodeBC) * table.size(), cudaMemcpyHostToDevice,
+                               m->stream));
+    }
+    if (m->N > 0)
+      NSM_CUDA(cudaMemcpyAsync(d_slot, slot.data(), sizeof(int) * m->N, cudaMemcpyHostToDevice, m->stream));
+    NSM_CUDA(cudaStreamSynchronize(m->stream));  // host vectors go out of scope
+  }
+  m->bcs_dirty = false;
+  return NSM_OK;
+}
+
+double* field_ptr(nsm_model* m, int field)
+{
+  switch (field) {
+    case NSM_FIELD_REFERENCE_COORDINATE: return m->d_X;
+    case NSM_FIELD_DISPLACEMENT: return m->d_u;
+    case NSM_FIELD_VELOCITY: return m->d_v;
+    case NSM_FIELD_ACCELERATION: return m->d_a;
+    case NSM_FIELD_INTERNAL_FORCE: return m->d_f;
+    case NSM_FIELD_EXTERNAL_FORCE: return m->d_fext;
+    default: return nullptr;
+  }
+}
+
+nsm::ElementArgs element_args(nsm_model* m, int k)
+{
+  nsm::ElementArgs a;
+  a.E         = m->E;
+  a.ld_e      = m->ld_e;
+  a.ld_n      = m->ld_n;
+  a.conn      = m->d_conn;
+  a.u         = m->d_u;
+  a.X         = m->d_X;
+  a.geo       = m->d_geo;
+  a.bulk      = m->K;
+  a.shear     = m->G;
+  a.F         = m->d_F;
+  a.sigma     = m->d_sigma;
+  a.fe        = m->d_fe;
+  a.store_ip  = (k < 0 || m->store_ip) ? 1 : 0;
+  a.sched     = k < 0 ? nullptr : m->d_sched;
+  a.step_base = m->d_step_base;
+  a.k         = k;
+  a.status    = m->d_status;
+  return a;
+}
+
+nsm::NodeArgs node_args(nsm_model* m, int k_post, int k_pre, int gather_only)
+{
+  nsm::NodeArgs a;
+  a.N           = m->N;
+  a.ld_n        = m->ld_n;
+  a.ld_e        = m->ld_e;
+  a.node_ptr    = m->d_node_ptr;
+  a.node_inc    = m->d_node_inc;
+  a.fe          = m->d_fe;
+  a.fe_is_float = m->precision == NSM_PRECISION_FP64 ? 0 : 1;
+  a.inv_mass    = m->d_inv_mass;
+  a.bc_slot     = m->d_bc_slot;
+  a.bcs         = m->d_bcs;
+  a.sched       = m->d_sched;
+  a.step_base   = m->d_step_base;
+  a.k_post      = k_post;
+  a.k_pre       = k_pre;
+  a.gather_only = gather_only;
+  a.u           = m->d_u;
+  a.v           = m->d_v;
+  a.a           = m->d_a;
+  a.f_int       = m->d_f;
+  return a;
+}
+
+cudaError_t launch_element(nsm_model* m, int k)
+{
+  nsm::ElementArgs a = element_args(m, k);
+  return m->precision == NSM_PRECISION_FP64 ? nsm::launch_element_fp64(a, m->stream)
+                                            : nsm::launch_element_fp32(a, m->stream);
+}
+
+std::pair<cudaEvent_t, cudaEvent_t> next_events(std::vector<std::pair<cudaEvent_t, cudaEvent_t>>& pool, size_t& used)
+{
+  if (used == pool.size()) {
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    pool.push_back({a, b});
+  }
+  return pool[used++];
+}
+
+// Launch sequence of a chunk of K schedule steps starting at the device base:
+// node(pre 0); {element(k); node(post k, pre k+1)}; node(post K-1); base += K.
+cudaError_t enqueue_chunk(nsm_model* m, int K, bool timed)
+{
+  cudaError_t e;
+  if ((e = nsm::launch_node_update(node_args(m, -1, 0, 0), m->stream)) != cudaSuccess) return e;
+  for (int k = 0; k < K; k++) {
+    if (timed) {
+      auto ev = next_events(m->ev_elem, m->ev_elem_used);
+      cudaEventRecord(ev.first, m->stream);
+      if ((e = launch_element(m, k)) != cudaSuccess) return e;
+      cudaEventRecord(ev.second, m->stream);
+      auto en = next_events(m->ev_node, m->ev_node_used);
+      cudaEventRecord(en.first, m->stream);
+      if ((e = nsm::launch_node_update(node_args(m, k, k + 1 < K ? k + 1 : -1, 0), m->stream)) != cudaSuccess)
+        return e;
+      cudaEventRecord(en.second, m->stream);
+    } else {
+      if ((e = launch_element(m, k)) != cudaSuccess) return e;
+      if ((e = nsm::launch_node_update(node_args(m, k, k + 1 < K ? k + 1 : -1, 0), m->stream)) != cudaSuccess)
+        return e;
+    }
+  }
+  return nsm::launch_advance_base(m->d_step_base, K, m->stream);
+}
+
+int get_graph(nsm_model* m, int K, cudaGraphExec_t* out)
+{
+  auto it = m->graphs.find(K);
+  if (it != m->graphs.end()) {
+    *out = it->second;
+    return NSM_OK;
+  }
+  cudaGraph_t graph;
+  NSM_CUDA(cudaStreamBeginCapture(m->stream, cudaStreamCaptureModeThreadLocal));
+  cudaError_t e  = enqueue_chunk(m, K, false);
+  cudaError_t e2 = cudaStreamEndCapture(m->stream, &graph);
+  if (e != cudaSuccess) return cuda_fail(e, "capture");
+  if (e2 != cudaSuccess) return cuda_fail(e2, "cudaStreamEndCapture");
+  cudaGraphExec_t exec;
+  e = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+  m->graphs[K] = exec;
+  *out         = exec;
+  return NSM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* nsm_last_error(void) { return g_error.c_str(); }
+int         nsm_abi_version(void) { return NSM_ABI_VERSION; }
+
+int nsm_create(const nsm_mesh_desc* mesh, const nsm_neohookean* material, const nsm_options* options,
+               nsm_model** out)
+{
+  if (!mesh || !material || !out) return fail(NSM_ERR_INVALID_ARGUMENT, "null argument");
+  *out = nullptr;
+  if (mesh->num_nodes < 0 || mesh->num_elem < 0 || (mesh->num_elem > 0 && (!mesh->coords || !mesh->conn)))
+    return fail(NSM_ERR_INVALID_ARGUMENT, "invalid mesh");
+  if (!(material->density > 0) || !(material->bulk_modulus > 0) || !(material->shear_modulus >= 0))
+    return fail(NSM_ERR_INVALID_ARGUMENT, "invalid neo-Hookean parameters");
+  const int N = mesh->num_nodes, E = mesh->num_elem;
+  for (long i = 0; i < 8L * E; i++)
+    if (mesh->conn[i] < 0 || mesh->conn[i] >= N) return fail(NSM_ERR_INVALID_ARGUMENT, "connectivity out of range");
+
+  nsm_model* m = new nsm_model();
+  m->N = N;
+  m->E = E;
+  m->ld_n = pad(N > 0 ? N : 1, 64);
+  m->ld_e = pad(E > 0 ? E : 1, 64);
+  if (options) {
+    m->precision   = options->precision;
+    m->store_ip    = options->store_ip_data;
+    m->device      = options->device;
+    m->graph_steps = options->graph_steps > 0 ? options->graph_steps : 50;
+  }
+  if (m->precision != NSM_PRECISION_FP64 && m->precision != NSM_PRECISION_FP32_MIXED) {
+    delete m;
+    return fail(NSM_ERR_INVALID_ARGUMENT, "unknown precision");
+  }
+  m->density = material->density;
+  m->K       = material->bulk_modulus;
+  m->G       = material->shear_modulus;
+
+  auto bail = [&](int code) {
+    free_all(m);
+    delete m;
+    return code;
+  };
+#define NSM_CUDA_B(call)                                       \
+  do {                                                         \
+    cudaError_t _e = (call);                                   \
+    if (_e != cudaSuccess) return bail(cuda_fail(_e, #call));  \
+  } while (0)
+
+  NSM_CUDA_B(cudaSetDevice(m->device));
+  NSM_CUDA_B(cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking));
+  const size_t nb = sizeof(double) * 3 * m->ld_n, eb = m->elem_bytes();
+  NSM_CUDA_B(cudaMalloc(&m->d_conn, sizeof(int) * 8 * m->ld_e));
+  NSM_CUDA_B(cudaMalloc(&m->d_node_ptr, sizeof(int) * (N + 1)));
+  NSM_CUDA_B(cudaMalloc(&m->d_node_inc, sizeof(int) * (8L * E > 0 ? 8L * E : 1)));
+  double** nodal[] = {&m->d_X, &m->d_u, &m->d_v, &m->d_a, &m->d_f, &m->d_fext};
+  for (double** p : nodal) {
+    NSM_CUDA_B(cudaMalloc(p, nb));
+    NSM_CUDA_B(cudaMemsetAsync(*p, 0, nb, m->stream));
+  }
+  NSM_CUDA_B(cudaMalloc(&m->d_mass, sizeof(double) * m->ld_n));
+  NSM_CUDA_B(cudaMalloc(&m->d_inv_mass, sizeof(double) * m->ld_n));
+  NSM_CUDA_B(cudaMalloc(&m->d_geo, sizeof(double) * 80 * m->ld_e));
+  NSM_CUDA_B(cudaMalloc(&m->d_F, eb * 72 * m->ld_e));
+  NSM_CUDA_B(cudaMalloc(&m->d_sigma, eb * 48 * m->ld_e));
+  NSM_CUDA_B(cudaMalloc(&m->d_fe, eb * 24 * m->ld_e));
+  NSM_CUDA_B(cudaMemsetAsync(m->d_F, 0, eb * 72 * m->ld_e, m->stream));
+  NSM_CUDA_B(cudaMemsetAsync(m->d_sigma, 0, eb * 48 * m->ld_e, m->stream));
+  NSM_CUDA_B(cudaMemsetAsync(m->d_fe, 0, eb * 24 * m->ld_e, m->stream));
+  NSM_CUDA_B(cudaMalloc(&m->d_status, sizeof(int)));
+  NSM_CUDA_B(cudaMemsetAsync(m->d_status, 0, sizeof(int), m->stream));
+  NSM_CUDA_B(cudaMalloc(&m->d_step_base, sizeof(int)));
+  NSM_CUDA_B(cudaMemsetAsync(m->d_step_base, 0, sizeof(int), m->stream));
+  NSM_CUDA_B(cudaMalloc(&m->d_out, sizeof(double) * 8));
+  NSM_CUDA_B(cudaMalloc(&m->d_stage, nb));
+  size_t scratch = sizeof(double) * (E > 0 ? (size_t)E : 1);
+  if (scratch < sizeof(double) * 2 * nsm::kEnergyBlocks) scratch = sizeof(double) * 2 * nsm::kEnergyBlocks;
+  NSM_CUDA_B(cudaMalloc(&m->d_scratch, scratch + sizeof(double) * 1024));
+
+  // host layouts -> device planes
+  {
+    std::vector<int> conn_soa((size_t)8 * m->ld_e, 0);
+    for (long e = 0; e < E; e++)
+      for (int c = 0; c < 8; c++) conn_soa[(size_t)c * m->ld_e + e] = mesh->conn[8 * e + c];
+    std::vector<double> X((size_t)3 * m->ld_n, 0.0);
+    for (long n = 0; n < N; n++)
+      for (int k = 0; k < 3; k++) X[(size_t)k * m->ld_n + n] = mesh->coords[3 * n + k];
+    // node -> (element, corner) incidence in increasing element order
+    std::vector<int> ptr(N + 1, 0), inc((size_t)8 * E);
+    for (long i = 0; i < 8L * E; i++) ptr[mesh->conn[i] + 1]++;
+    for (int n = 0; n < N; n++) ptr[n + 1] += ptr[n];
+    std::vector<int> fill(ptr.begin(), ptr.end() - 1);
+    for (long i = 0; i < 8L * E; i++) inc[fill[mesh->conn[i]]++] = (int)i;
+    NSM_CUDA_B(cudaMemcpyAsync(m->d_conn, conn_soa.data(), sizeof(int) * conn_soa.size(), cudaMemcpyHostToDevice,
+                               m->stream));
+    NSM_CUDA_B(cudaMemcpyAsync(m->d_X, X.data(), sizeof(double) * X.size(), cudaMemcpyHostToDevice, m->stream));
+    NSM_CUDA_B(cudaMemcpyAsync(m->d_node_ptr, ptr.data(), sizeof(int) * ptr.size(), cudaMemcpyHostToDevice,
+                               m->stream));
+    if (E > 0)
+      NSM_CUDA_B(cudaMemcpyAsync(m->d_node_inc, inc.data(), sizeof(int) * inc.size(), cudaMemcpyHostToDevice,
+                                 m->stream));
+    NSM_CUDA_B(nsm::upload_shape_tables(m->stream));
+
+    // setup: geometry, lumped mass, critical time step
+    double* me = nullptr;
+    NSM_CUDA_B(cudaMalloc(&me, sizeof(double) * 8 * m->ld_e));
+    nsm::SetupArgs s;
+    s.N = N;
+    s.E = E;
+    s.ld_n = m->ld_n;
+    s.ld_e = m->ld_e;
+    s.conn = m->d_conn;
+    s.X = m->d_X;
+    s.node_ptr = m->d_node_ptr;
+    s.node_inc = m->d_node_inc;
+    s.density = m->density;
+    s.sound_speed = std::sqrt(m->K / m->density);
+    s.geo = m->d_geo;
+    s.me = me;
+    s.dt_elem = m->d_scratch;
+    s.dt_partial = m->d_scratch + (scratch / sizeof(double));
+    s.dt_out = m->d_out;
+    s.mass = m->d_mass;
+    s.inv_mass = m->d_inv_mass;
+    s.status = m->d_status;
+    cudaError_t e = (E > 0) ? nsm::launch_setup(s, m->stream) : cudaSuccess;
+    double      dt = 1.7976931348623157e308;
+    if (e == cudaSuccess && E > 0) e = cudaMemcpyAsync(&dt, m->d_out, sizeof(double), cudaMemcpyDeviceToHost, m->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(m->stream);  // host vectors live until here
+    cudaFree(me);
+    if (e != cudaSuccess) return bail(cuda_fail(e, "setup"));
+    m->dt_crit = dt;
+  }
+  int st = read_status(m);
+  if (st != NSM_OK) return bail(st);
+  int bc = upload_bcs(m);
+  if (bc != NSM_OK) return bail(bc);
+#undef NSM_CUDA_B
+  *out = m;
+  return NSM_OK;
+}
+
+int nsm_destroy(nsm_model* m)
+{
+  if (!m) return NSM_OK;
+  cudaSetDevice(m->device);
+  if (m->stream) cudaStreamSynchronize(m->stream);
+  free_all(m);
+  delete m;
+  return NSM_OK;
+}
+
+int nsm_add_boundary_condition(nsm_model* m, int kind, int component, double value, const int* nodes, int count)
+{
+  if (!m || (count > 0 && !nodes)) return fail(NSM_ERR_INVALID_ARGUMENT, "null argument");
+  if (kind < NSM_BC_INITIAL_VELOCITY || kind > NSM_BC_PRESCRIBED_DISPLACEMENT)
+    return fail(NSM_ERR_INVALID_ARGUMENT, "unknown boundary condition kind");
+  if (component < 0 || component > 2) return fail(NSM_ERR_INVALID_ARGUMENT, "unknown coordinate");
+  BcLine b{kind, component, value, std::vector<int>(nodes, nodes + count)};
+  for (int n : b.nodes)
+    if (n < 0 || n >= m->N) return fail(NSM_ERR_INVALID_ARGUMENT, "node set entry out of range");
+  m->bcs.push_back(std::move(b));
+  m->bcs_dirty = true;
+  return upload_bcs(m);
+}
+
+int nsm_compute_lumped_mass(nsm_model* m, double* mass)
+{
+  if (!m) return fail(NSM_ERR_INVALID_ARGUMENT, "null model");
+  NSM_CUDA(cudaSetDevice(m->device));
+  if (mass && m->N > 0) {
+    NSM_CUDA(cudaMemcpyAsync(mass, m->d_mass, sizeof(double) * m->N, cudaMemcpyDeviceToHost, m->stream));
+    NSM_CUDA(cudaStreamSynchronize(m->stream));
+  }
+  return NSM_OK;
+}
+
+int nsm_critical_time_step(nsm_model* m, double* dt)
+{
+  if (!m || !dt) return fail(NSM_ERR_INVALID_ARGUMENT, "null argument");
+  *dt = m->dt_crit;
+  return NSM_OK;
+}
+
+int nsm_apply_initial_conditions(nsm_model* m)
+{
+  if (!m) return fail(NSM_ERR_INVALID_ARGUMENT, "null model");
+  NSM_CUDA(cudaSetDevice(m->device));
+  int r = upload_bcs(m);
+  if (r) return r;
+  if (m->d_ibcs) NSM_CUDA(nsm::launch_apply_bc(m->N, m->ld_n, m->d_ibc_slot, m->d_ibcs, 0.0, m->d_u, m->d_v, m->stream));
+  return NSM_OK;
+}
+
+int nsm_apply_kinematic_conditions(nsm_model* m, double t_cur, double t_prev)
+{
+  if (!m) return fail(NSM_ERR_INVALID_ARGUMENT, "null model");
+  NSM_CUDA(cudaSetDevice(m->device));
+  int r = upload_bcs(m);
+  if (r) return r;
+  if (m->d_bcs)
+    NSM_CUDA(nsm::launch_apply_bc(m->N, m->ld_n, m->d_bc_slot, m->d_bcs, t_cur - t_prev, m->d_u, m->d_v, m->stream));
+  return NSM_OK;
+}
+
+int nsm_set_node_field(nsm_model* m, int field, const double* values)
+{
+  if (!m || !values) return fail(NSM_ERR_INVALID_ARGUMENT, "null argument");
+  double* dst = field_ptr(m, field);
+  if (!dst) return fail(NSM_ERR_INVALID_ARGUMENT, "unknown field");
+  if (field == NSM_FIELD_REFERENCE_COORDINATE) return fail(NSM_ERR_INVALID_ARGUMENT, "reference coordinates are fixed");
+  NSM_CUDA(cudaSetDevice(m->device));
+  if (m->N == 0) return NSM_OK;
+  NSM_CUDA(cudaMemcpyAsync(m->d_stage, values, sizeof(double) * 3 * m->N, cudaMemcpyHostToDevice, m->stream));
+  NSM_CUDA(nsm::launch_node_aos_to_soa(m->N, m->ld_n, m->d_stage, dst, m->stream));
+  NSM_CUDA(cudaStreamSynchronize(m->stream));
+  return NSM_OK;
+}
+
+int nsm_get_node_field(nsm_model* m, int field, double* values)
+{
+  if (!m || !values) return fail(NSM_ERR_INVALID_ARGUMENT, "null argument");
+  double* src = field_ptr(m, field);
+  if (!src) return fail(NSM_ERR_INVALID_ARGUMENT, "unknown field");
+  NSM_CUDA(cudaSetDevice(m->device));
+  if (m->N == 0) return NSM_OK;
+  NSM_CUDA(nsm::launch_node_soa_to_aos(m->N, m->ld_n, src, m->d_stage, m->stream));
+  NSM_CUDA(cudaMemcpyAsync(values, m->d_stage, sizeof(double) * 3 * m->N, cudaMemcpyDeviceToHost, m->stream));
+  NSM_CUDA(cudaStreamSynchronize(m->stream));
+  return NSM_OK;
+}
+
+int nsm_compute_internal_force(nsm_model* m, double, double, int)
+{
+  if (!m) return fail(NSM_ERR_INVALID_ARGUMENT, "null model");
+  NSM_CUDA(cudaSetDevice(m->device));
+  NSM_CUDA(launch_element(m, -1));
+  NSM_CUDA(nsm::launch_node_update(node_args(m, -1, -1, 1), m->stream));
+  return read_status(m);
+}
+
+int nsm_compute_internal_force_host(nsm_model* m, const double* displacement, double* internal_force)
+{
+  if (!m || !displacement || !internal_force) return fail(NSM_ERR_INVALID_ARGUMENT, "null argument");
+  NSM_CUDA(cudaSetDevice(m->device));
+  if (m->N == 0) return NSM_OK;
+  const size_t bytes = sizeof(double) * 3 * m->N;
+  NSM_CUDA(cudaMemcpyAsync(m->d_stage, displacement, bytes, cudaMemcpyHostToDevice, m->stream));
+  NSM_CUDA(nsm::launch_node_aos_to_soa(m->N, m->ld_n, m->d_stage, m->d_u, m->stream));
+  NSM_CUDA(launch_element(m, -1));
+  NSM_CUDA(nsm::launch_node_update(node_args(m, -1, -1, 1), m->stream));
+  NSM_CUDA(nsm::launch_node_soa_to_aos(m->N, m->ld_n, m->d_f, m->d_stage, m->stream));
+  NSM_CUDA(cudaMemcpyAsync(internal_force, m->d_stage, bytes, cudaMemcpyDeviceToHost, m->stream));
+  return read_status(m);  // synchronizes
+}
+
+int nsm_get_ip_data(nsm_model* m, double* F, double* sigma)
+{
+  if (!m) return fail(NSM_ERR_INVALID_ARGUMENT, "null model");
+  NSM_CUDA(cudaSetDevice(m->device));
+  if (m->E == 0) return NSM_OK;
+  const int is_float = m->precision == NSM_PRECISION_FP64 ? 0 : 1;
+  double*   tmp      = nullptr;
+  NSM_CUDA(cudaMalloc(&tmp, sizeof(double) * 72 * (size_t)m->E));
+  cudaError_t e = cudaSuccess;
+  if (F) {
+    e = nsm::launch_ip_to_aos(m->E, m->ld_e, m->d_F, is_float, 9, tmp, m->stream);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(F, tmp, sizeof(double) * 72 * (size_t)m->E, cudaMemcpyDeviceToHost, m->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(m->stream);
+  }
+  if (sigma && e == cudaSuccess) {
+    e = nsm::launch_ip_to_aos(m->E, m->ld_e, m->d_sigma, is_float, 6, tmp, m->stream);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(sigma, tmp, sizeof(double) * 48 * (size_t)m->E, cudaMemcpyDeviceToHost, m->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(m->stream);
+  }
+  cudaFree(tmp);
+  if (e != cudaSuccess) return cuda_fail(e, "nsm_get_ip_data");
+  return NSM_OK;
+}
+
+int nsm_get_energies(nsm_model* m, double* kinetic, double* internal)
+{
+  if (!m) return fail(NSM_ERR_INVALID_ARGUMENT, "null model");
+  NSM_CUDA(cudaSetDevice(m->device));
+  NSM_CUDA(nsm::launch_energies(m->N, m->ld_n, m->d_mass, m->d_v, m->E, m->ld_e, m->d_conn, m->d_u, m->d_geo, m->K,
+                                m->G, m->d_scratch, m->d_out + 2, m->stream));
+  double out[2];
+  NSM_CUDA(cudaMemcpyAsync(out, m->d_out + 2, sizeof(out), cudaMemcpyDeviceToHost, m->stream));
+  NSM_CUDA(cudaStreamSynchronize(m->stream));
+  if (kinetic) *kinetic = out[0];
+  if (internal) *internal = out[1];
+  return NSM_OK;
+}
+
+int nsm_begin(nsm_model* m, double initial_time, double final_time, int num_steps, int output_frequency,
+              const double* v_init)
+{
+  if (!m) return fail(NSM_ERR_INVALID_ARGUMENT, "null model");
+  if (num_steps < 0 || output_frequency < 0) return fail(NSM_ERR_INVALID_ARGUMENT, "negative step count");
+  if (final_time < initial_time) return fail(NSM_ERR_INVALID_ARGUMENT, "final time is less than initial time");
+  NSM_CUDA(cudaSetDevice(m->device));
+  // schedule as src/integrators/explicit_time_integrator.cc:130-199 forms it
+  m->h_sched.assign(num_steps > 0 ? num_steps : 1, StepSched{0, 0, 0, 0});
+  m->h_time.assign(num_steps + 1, initial_time);
+  double t_cur = initial_time, t_prev = initial_time;
+  double dt_user = num_steps > 0 ? (final_time - initial_time) / num_steps : 0.0;
+  for (int s = 0; s < num_steps; s++) {
+    t_prev = t_cur;
+    t_cur += dt_user;
+    StepSched& q = m->h_sched[s];
+    q.delta      = t_cur - t_prev;
+    q.half       = 0.5 * q.delta;
+    q.is_output  = (output_frequency != 0 && (s % output_frequency == 0 || s == num_steps - 1)) ? 1 : 0;
+    m->h_time[s + 1] = t_cur;
+  }
+  if (m->d_sched) cudaFree(m->d_sched);
+  m->d_sched = nullptr;
+  NSM_CUDA(cudaMalloc(&m->d_sched, sizeof(StepSched) * m->h_sched.size()));
+  NSM_CUDA(cudaMemcpyAsync(m->d_sched, m->h_sched.data(), sizeof(StepSched) * m->h_sched.size(),
+                           cudaMemcpyHostToDevice, m->stream));
+  // graphs hold the schedule pointer: rebuild them
+  for (auto& g : m->graphs) cudaGraphExecDestroy(g.second);
+  m->graphs.clear();
+  NSM_CUDA(cudaMemsetAsync(m->d_step_base, 0, sizeof(int), m->stream));
+  const size_t nb = sizeof(double) * 3 * m->ld_n;
+  NSM_CUDA(cudaMemsetAsync(m->d_u, 0, nb, m->stream));
+  NSM_CUDA(cudaMemsetAsync(m->d_v, 0, nb, m->stream));
+  NSM_CUDA(cudaMemsetAsync(m->d_a, 0, nb, m->stream));
+  NSM_CUDA(cudaMemsetAsync(m->d_f, 0, nb, m->stream));
+  int r = nsm_apply_initial_conditions(m);
+  if (r) return r;
+  if (v_init) {
+    r = nsm_set_node_field(m, NSM_FIELD_VELOCITY, v_init);
+    if (r) return r;
+  }
+  r = nsm_apply_kinematic_conditions(m, initial_time, initial_time);
+  if (r) return r;
+  NSM_CUDA(cudaStreamSynchronize(m->stream));
+  m->num_steps  = num_steps;
+  m->steps_done = 0;
+  m->t0         = initial_time;
+  m->begun      = true;
+  return NSM_OK;
+}
+
+int nsm_advance(nsm_model* m, int num_steps)
+{
+  if (!m) return fail(NSM_ERR_INVALID_ARGUMENT, "null model");
+  if (!m->begun) return fail(NSM_ERR_STATE, "nsm_advance before nsm_begin");
+  if (num_steps < 0 || m->steps_done + num_steps > m->num_steps)
+    return fail(NSM_ERR_INVALID_ARGUMENT, "advance past the end of the schedule");
+  NSM_CUDA(cudaSetDevice(m->device));
+  while (num_steps > 0) {
+    int K = num_steps < m->graph_steps ? num_steps : m->graph_steps;
+    if (m->profiling) {
+      NSM_CUDA(enqueue_chunk(m, K, true));
+    } else {
+      cudaGraphExec_t exec;
+      int             r = get_graph(m, K, &exec);
+      if (r) return r;
+      NSM_CUDA(cudaGraphLaunch(exec, m->stream));
+    }
+    m->steps_done += K;
+    num_steps -= K;
+  }
+  return NSM_OK;
+}
+
+int nsm_advance_timed(nsm_model* m, int num_steps, double* device_ms)
+{
+  if (!m || !device_ms) return fail(NSM_ERR_INVALID_ARGUMENT, "null argument");
+  NSM_CUDA(cudaSetDevice(m->device));
+  cudaEvent_t a, b;
+  NSM_CUDA(cudaEventCreate(&a));
+  NSM_CUDA(cudaEventCreate(&b));
+  NSM_CUDA(cudaEventRecord(a, m->stream));
+  int r = nsm_advance(m, num_steps);
+  cudaEventRecord(b, m->stream);
+  cudaError_t e = cudaEventSynchronize(b);
+  float       ms = 0.0f;
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  if (r) return r;
+  if (e != cudaSuccess) return cuda_fail(e, "nsm_advance_timed");
+  *device_ms = ms;
+  return read_status(m);
+}
+
+int nsm_progress(nsm_model* m, int* steps_done, double* time_current)
+{
+  if (!m) return fail(NSM_ERR_INVALID_ARGUMENT, "null model");
+  if (steps_done) *steps_done = m->steps_done;
+  if (time_current) *time_current = m->begun ? m->h_time[m->steps_done] : 0.0;
+  return NSM_OK;
+}
+
+int nsm_synchronize(nsm_model* m)
+{
+  if (!m) return fail(NSM_ERR_INVALID_ARGUMENT, "null model");
+  NSM_CUDA(cudaSetDevice(m->device));
+  NSM_CUDA(cudaStreamSynchronize(m->stream));
+  return NSM_OK;
+}
+
+int nsm_check_status(nsm_model* m)
+{
+  if (!m) return fail(NSM_ERR_INVALID_ARGUMENT, "null model");
+  NSM_CUDA(cudaSetDevice(m->device));
+  return read_status(m);
+}
+
+int nsm_time_kernels(nsm_model* m, int repeats, double* element_ms, double* node_ms)
+{
+  if (!m || repeats <= 0) return fail(NSM_ERR_INVALID_ARGUMENT, "invalid argument");
+  NSM_CUDA(cudaSetDevice(m->device));
+  cudaEvent_t a, b, c;
+  NSM_CUDA(cudaEventCreate(&a));
+  NSM_CUDA(cudaEventCreate(&b));
+  NSM_CUDA(cudaEventCreate(&c));
+  cudaEventRecord(a, m->stream);
+  for (int r = 0; r < repeats; r++) NSM_CUDA(launch_element(m, -1));
+  cudaEventRecord(b, m->stream);
+  for (int r = 0; r < repeats; r++) NSM_CUDA(nsm::launch_node_update(node_args(m, -1, -1, 1), m->stream));
+  cudaEventRecord(c, m->stream);
+  NSM_CUDA(cudaEventSynchronize(c));
+  float ms1 = 0, ms2 = 0;
+  cudaEventElapsedTime(&ms1, a, b);
+  cudaEventElapsedTime(&ms2, b, c);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaEventDestroy(c);
+  if (element_ms) *element_ms = ms1 / repeats;
+  if (node_ms) *node_ms = ms2 / repeats;
+  return read_status(m);
+}
+
+int nsm_launches_per_advance(nsm_model* m, int num_steps)
+{
+  if (!m || num_steps < 0) return -1;
+  int launches = 0;
+  while (num_steps > 0) {
+    int K = num_steps < m->graph_steps ? num_steps : m->graph_steps;
+    launches += 2 + 2 * K;
+    num_steps -= K;
+  }
+  return launches;
+}
+
+// Profiling mode: nsm_advance launches without graphs and brackets every
+// element and node kernel with CUDA events on the model's stream.
+int nsm_set_profiling(nsm_model* m, int enable)
+{
+  if (!m) return fail(NSM_ERR_INVALID_ARGUMENT, "null model");
+  m->profiling    = enable != 0;
+  m->ev_elem_used = 0;
+  m->ev_node_used = 0;
+  return NSM_OK;
+}
+
+int nsm_get_profile(nsm_model* m, double* element_ms_total, int* element_launches, double* node_ms_total,
+                    int* node_launches)
+{
+  if (!m) return fail(NSM_ERR_INVALID_ARGUMENT, "null model");
+  NSM_CUDA(cudaSetDevice(m->device));
+  NSM_CUDA(cudaStreamSynchronize(m->stream));
+  double te = 0, tn = 0;
+  for (size_t i = 0; i < m->ev_elem_used; i++) {
+    float ms = 0;
+    NSM_CUDA(cudaEventElapsedTime(&ms, m->ev_elem[i].first, m->ev_elem[i].second));
+    te += ms;
+  }
+  for (size_t i = 0; i < m->ev_node_used; i++) {
+    float ms = 0;
+    NSM_CUDA(cudaEventElapsedTime(&ms, m->ev_node[i].first, m->ev_node[i].second));
+    tn += ms;
+  }
+  if (element_ms_total) *element_ms_total = te;
+  if (element_launches) *element_launches = (int)m->ev_elem_used;
+  if (node_ms_total) *node_ms_total = tn;
+  if (node_launches) *node_launches = (int)m->ev_node_used;
+  m->ev_elem_used = 0;
+  m->ev_node_used = 0;
+  return NSM_OK;
+}
+
+void* nsm_host_alloc(size_t bytes)
+{
+  void* p = nullptr;
+  if (cudaMallocHost(&p, bytes) != cudaSuccess) {
+    g_error = "cudaMallocHost failed";
+    return nullptr;
+  }
+  return p;
+}
+
+void nsm_host_free(void* p)
+{
+  if (p) cudaFreeHost(p);
+}
+
+}  // extern "C"

@@ -1,0 +1,277 @@
+"""Python binding of the engine's C ABI (include/nimble_gb300.h).
+
+`Model` mirrors the reference's ModelDataBase interface for one block
+(src/nimble_model_data_base.h:87-345: ComputeLumpedMass, GetCriticalTimeStep,
+ApplyInitialConditions, ApplyKinematicConditions, ComputeInternalForce,
+GetVectorNodeData, ...) and adds the device-resident explicit loop of
+ExplicitTimeIntegrator::Integrate (src/integrators/explicit_time_integrator.cc:61-325)
+as `begin` / `advance`.  Every call goes through libnimble_gb300.so; there is
+no other implementation behind it, and a missing library is an ImportError.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from .mesh import Problem
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libnimble_gb300.so")
+
+NSM_OK = 0
+ERRORS = {1: "invalid argument", 2: "CUDA error", 3: "non-positive Jacobian", 4: "non-finite force",
+          5: "call out of order", 6: "out of memory"}
+PRECISION = {"fp64": 0, "fp32": 1, "fp32_mixed": 1}
+FIELDS = {"reference_coordinate": 0, "displacement": 1, "velocity": 2, "acceleration": 3,
+          "internal_force": 4, "external_force": 5}
+
+
+class EngineError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class _Mesh(C.Structure):
+    _fields_ = [("num_nodes", C.c_int), ("num_elem", C.c_int), ("coords", C.POINTER(C.c_double)),
+                ("conn", C.POINTER(C.c_int))]
+
+
+class _Material(C.Structure):
+    _fields_ = [("density", C.c_double), ("bulk_modulus", C.c_double), ("shear_modulus", C.c_double)]
+
+
+class _Options(C.Structure):
+    _fields_ = [("precision", C.c_int), ("store_ip_data", C.c_int), ("device", C.c_int),
+                ("graph_steps", C.c_int)]
+
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+_vp = C.c_void_p
+
+# name -> (restype, argtypes); kept in step with include/nimble_gb300.h
+SIGNATURES = {
+    "nsm_last_error": (C.c_char_p, []),
+    "nsm_abi_version": (C.c_int, []),
+    "nsm_create": (C.c_int, [C.POINTER(_Mesh), C.POINTER(_Material), C.POINTER(_Options), C.POINTER(_vp)]),
+    "nsm_destroy": (C.c_int, [_vp]),
+    "nsm_add_boundary_condition": (C.c_int, [_vp, C.c_int, C.c_int, C.c_double, _ip, C.c_int]),
+    "nsm_compute_lumped_mass": (C.c_int, [_vp, _dp]),
+    "nsm_critical_time_step": (C.c_int, [_vp, _dp]),
+    "nsm_apply_initial_conditions": (C.c_int, [_vp]),
+    "nsm_apply_kinematic_conditions": (C.c_int, [_vp, C.c_double, C.c_double]),
+    "nsm_set_node_field": (C.c_int, [_vp, C.c_int, _dp]),
+    "nsm_get_node_field": (C.c_int, [_vp, C.c_int, _dp]),
+    "nsm_compute_internal_force": (C.c_int, [_vp, C.c_double, C.c_double, C.c_int]),
+    "nsm_compute_internal_force_host": (C.c_int, [_vp, _dp, _dp]),
+    "nsm_get_ip_data": (C.c_int, [_vp, _dp, _dp]),
+    "nsm_get_energies": (C.c_int, [_vp, _dp, _dp]),
+    "nsm_begin": (C.c_int, [_vp, C.c_double, C.c_double, C.c_int, C.c_int, _dp]),
+    "nsm_advance": (C.c_int, [_vp, C.c_int]),
+    "nsm_advance_timed": (C.c_int, [_vp, C.c_int, _dp]),
+    "nsm_progress": (C.c_int, [_vp, _ip, _dp]),
+    "nsm_synchronize": (C.c_int, [_vp]),
+    "nsm_check_status": (C.c_int, [_vp]),
+    "nsm_time_kernels": (C.c_int, [_vp, C.c_int, _dp, _dp]),
+    "nsm_launches_per_advance": (C.c_int, [_vp, C.c_int]),
+    "nsm_set_profiling": (C.c_int, [_vp, C.c_int]),
+    "nsm_get_profile": (C.c_int, [_vp, _dp, _ip, _dp, _ip]),
+    "nsm_host_alloc": (_vp, [C.c_size_t]),
+    "nsm_host_free": (None, [_vp]),
+}
+
+_lib = None
+
+
+def library():
+    """Loads libnimble_gb300.so (built by nimblesm_gb300.build)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: build it with nimblesm_gb300.build.build()")
+        lib = C.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+    return _lib
+
+
+def _check(rc):
+    if rc != NSM_OK:
+        raise EngineError(rc, library().nsm_last_error().decode())
+
+
+def _d(a):
+    return a.ctypes.data_as(_dp)
+
+
+class PinnedArray:
+    """A page-locked host array (nsm_host_alloc) viewed as numpy."""
+
+    def __init__(self, shape, dtype=np.float64):
+        self.shape = tuple(shape)
+        nbytes = int(np.prod(self.shape)) * np.dtype(dtype).itemsize
+        self._ptr = library().nsm_host_alloc(max(nbytes, 8))
+        if not self._ptr:
+            raise MemoryError("pinned allocation failed")
+        buf = (C.c_char * max(nbytes, 8)).from_address(self._ptr)
+        self.array = np.frombuffer(buf, dtype=dtype, count=int(np.prod(self.shape))).reshape(self.shape)
+
+    def __del__(self):
+        if getattr(self, "_ptr", None):
+            library().nsm_host_free(self._ptr)
+            self._ptr = None
+
+
+class Model:
+    """Device-resident ModelData for one block of hex8 elements."""
+
+    def __init__(self, problem: Problem, precision: str = "fp64", store_ip_data: bool = True, device: int = 0,
+                 graph_steps: int = 50):
+        lib = library()
+        self.problem = problem
+        self.precision = precision
+        coords = np.ascontiguousarray(problem.coords, dtype=np.float64)
+        conn = np.ascontiguousarray(problem.conn, dtype=np.int32)
+        mesh = _Mesh(problem.num_nodes, problem.num_elem, _d(coords), conn.ctypes.data_as(_ip))
+        mat = _Material(problem.density, problem.bulk_modulus, problem.shear_modulus)
+        opt = _Options(PRECISION[precision], 1 if store_ip_data else 0, device, graph_steps)
+        h = _vp()
+        _check(lib.nsm_create(C.byref(mesh), C.byref(mat), C.byref(opt), C.byref(h)))
+        self._h = h
+        for bc in problem.bcs:
+            if bc.node_set not in problem.node_sets:
+                continue  # the reference drops lines naming an absent node set
+            nodes = np.ascontiguousarray(problem.node_sets[bc.node_set], dtype=np.int32)
+            _check(lib.nsm_add_boundary_condition(h, bc.kind, bc.component, bc.value,
+                                                  nodes.ctypes.data_as(_ip), len(nodes)))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            library().nsm_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    # ---- ModelDataBase mirror ----
+    def ComputeLumpedMass(self) -> np.ndarray:
+        m = np.zeros(self.problem.num_nodes)
+        _check(library().nsm_compute_lumped_mass(self._h, _d(m)))
+        return m
+
+    def GetCriticalTimeStep(self) -> float:
+        dt = C.c_double()
+        _check(library().nsm_critical_time_step(self._h, C.byref(dt)))
+        return dt.value
+
+    def ApplyInitialConditions(self):
+        _check(library().nsm_apply_initial_conditions(self._h))
+
+    def ApplyKinematicConditions(self, time_current, time_previous):
+        _check(library().nsm_apply_kinematic_conditions(self._h, time_current, time_previous))
+
+    def GetVectorNodeData(self, label) -> np.ndarray:
+        out = np.zeros((self.problem.num_nodes, 3))
+        _check(library().nsm_get_node_field(self._h, FIELDS[label], _d(out)))
+        return out
+
+    def SetVectorNodeData(self, label, values):
+        v = np.ascontiguousarray(values, dtype=np.float64)
+        assert v.shape == (self.problem.num_nodes, 3)
+        _check(library().nsm_set_node_field(self._h, FIELDS[label], _d(v)))
+
+    def ComputeInternalForce(self, time_previous=0.0, time_current=0.0, is_output_step=False):
+        _check(library().nsm_compute_internal_force(self._h, time_previous, time_current, int(is_output_step)))
+
+    def ComputeInternalForceHost(self, displacement, out=None) -> np.ndarray:
+        u = np.ascontiguousarray(displacement, dtype=np.float64)
+        f = out if out is not None else np.zeros((self.problem.num_nodes, 3))
+        _check(library().nsm_compute_internal_force_host(self._h, _d(u), _d(f)))
+        return f
+
+    def GetIntegrationPointData(self):
+        E = self.problem.num_elem
+        F, s = np.zeros((E, 8, 9)), np.zeros((E, 8, 6))
+        _check(library().nsm_get_ip_data(self._h, _d(F), _d(s)))
+        return F, s
+
+    def GetEnergies(self):
+        ke, ie = C.c_double(), C.c_double()
+        _check(library().nsm_get_energies(self._h, C.byref(ke), C.byref(ie)))
+        return ke.value, ie.value
+
+    # ---- explicit loop ----
+    def begin(self, final_time, num_steps, output_frequency=0, initial_time=0.0, v_init="problem"):
+        if isinstance(v_init, str):
+            v_init = self.problem.v_init
+        v = None if v_init is None else np.ascontiguousarray(v_init, dtype=np.float64)
+        _check(library().nsm_begin(self._h, initial_time, final_time, num_steps, output_frequency,
+                                   None if v is None else _d(v)))
+
+    def advance(self, num_steps):
+        _check(library().nsm_advance(self._h, int(num_steps)))
+
+    def advance_timed(self, num_steps) -> float:
+        """Advances and returns the device milliseconds (CUDA events on the
+        engine's stream)."""
+        ms = C.c_double()
+        _check(library().nsm_advance_timed(self._h, int(num_steps), C.byref(ms)))
+        return ms.value
+
+    def synchronize(self):
+        _check(library().nsm_synchronize(self._h))
+        _check(library().nsm_check_status(self._h))
+
+    def progress(self):
+        s, t = C.c_int(), C.c_double()
+        _check(library().nsm_progress(self._h, C.byref(s), C.byref(t)))
+        return s.value, t.value
+
+    def state(self, with_ip=True):
+        """Post-step state in the reference layouts."""
+        self.synchronize()
+        out = {k: self.GetVectorNodeData(lbl) for k, lbl in
+               (("u", "displacement"), ("v", "velocity"), ("a", "acceleration"), ("f_int", "internal_force"))}
+        if with_ip:
+            out["F"], out["sigma"] = self.GetIntegrationPointData()
+        out["mass"] = self.ComputeLumpedMass()
+        out["steps"], out["time"] = self.progress()
+        return out
+
+    # ---- measurement helpers ----
+    def time_kernels(self, repeats=10):
+        e, n = C.c_double(), C.c_double()
+        _check(library().nsm_time_kernels(self._h, repeats, C.byref(e), C.byref(n)))
+        return e.value, n.value
+
+    def launches_per_advance(self, num_steps):
+        return library().nsm_launches_per_advance(self._h, int(num_steps))
+
+    def set_profiling(self, enable):
+        _check(library().nsm_set_profiling(self._h, int(bool(enable))))
+
+    def get_profile(self):
+        te, tn = C.c_double(), C.c_double()
+        ne, nn = C.c_int(), C.c_int()
+        _check(library().nsm_get_profile(self._h, C.byref(te), C.byref(ne), C.byref(tn), C.byref(nn)))
+        return {"element_ms": te.value, "element_launches": ne.value, "node_ms": tn.value,
+                "node_launches": nn.value}
+
+
+def run(problem: Problem, final_time: float, num_steps: int, output_frequency: int = 0,
+        precision: str = "fp64", with_ip=True) -> dict:
+    """Whole explicit run on the device; returns the final state."""
+    m = Model(problem, precision=precision)
+    m.begin(final_time, num_steps, output_frequency)
+    m.advance(num_steps)
+    out = m.state(with_ip=with_ip)
+    out["kinetic_energy"], out["internal_energy"] = m.GetEnergies()
+    out["dt_crit"] = m.GetCriticalTimeStep()
+    m.close()
+    return out

@@ -1,0 +1,224 @@
+"""Parity of the CUDA engine (through the C ABI) with the CPU oracle and the
+reference's gold files.
+
+Tolerance for the FP64 form: 1e-10 relative (normwise over the field) in
+nodal displacement, velocity and integration-point stress after N steps; the
+lumped mass and the critical time step are bit-exact (same arithmetic order,
+no FMA contraction).  FP32-mixed form: 1e-3 relative displacement error
+against the FP64 form."""
+import numpy as np
+import pytest
+
+from nimblesm_gb300 import engine as E
+from nimblesm_gb300.mesh import BC_PRESCRIBED_DISPLACEMENT, BoundaryCondition, cube_problem, critical_time_step
+from oracle import oracle as O
+from tests.goldens import exodiff_ok, gold_problem, load, output_steps
+from tests.gpu_util import rel
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-10
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    from nimblesm_gb300 import build as B
+    B.build()
+    O.build(ref=False)
+
+
+def compare(gpu, ref, keys=("u", "v", "sigma"), tol=TOL):
+    for k in keys:
+        e = rel(gpu[k], ref[k])
+        assert e <= tol, f"{k}: relative error {e:.3e}"
+
+
+def test_single_element_known_answers():
+    """Each reference element of the known-answer fixture, as a one-element
+    mesh: F, sigma and nodal forces against the reference's values."""
+    fx = load("ref_points")
+    for k in range(fx["elem_X"].shape[0]):
+        p = cube_problem(1)
+        p.coords = fx["elem_X"][k].copy()
+        p.bcs, p.v_init = [], None
+        p.bulk_modulus, p.shear_modulus = float(fx["K"]), float(fx["G"])
+        m = E.Model(p)
+        m.SetVectorNodeData("displacement", fx["elem_u"][k])
+        m.ComputeInternalForce()
+        f = m.GetVectorNodeData("internal_force")
+        F, s = m.GetIntegrationPointData()
+        assert rel(F, fx["elem_F"][k]) < 1e-13
+        assert rel(s, fx["elem_sigma"][k]) < 1e-9
+        assert rel(f, fx["elem_f"][k]) < 1e-9
+        m.close()
+
+
+@pytest.mark.parametrize("name", ["cube4_jitter", "cube16_cfg0"])
+def test_cube_against_reference_fixture(name):
+    fx = load("ref_" + name)
+    p = cube_problem(int(fx["n"]), jitter=float(fx["jitter"]), seed=int(fx["seed"]))
+    g = E.run(p, float(fx["final_time"]), int(fx["steps"]), int(fx["output_frequency"]))
+    assert g["dt_crit"] == float(fx["dt_crit"])
+    assert np.array_equal(g["mass"], fx["mass"])
+    idx = fx.get("elem_index")
+    ref = {k: fx[k] for k in ("u", "v", "a", "f_int")}
+    ref["sigma"] = fx["sigma"]
+    gs = g["sigma"] if idx is None else g["sigma"][idx]
+    compare({"u": g["u"], "v": g["v"], "sigma": gs}, ref)
+    assert rel(g["a"], fx["a"]) < 1e-9 and rel(g["f_int"], fx["f_int"]) < 1e-9
+    if idx is not None:
+        assert abs(np.linalg.norm(g["sigma"]) - float(fx["sigma_norm"])) <= 1e-10 * float(fx["sigma_norm"])
+
+
+@pytest.mark.parametrize("name", ["single_elem_native_neohookean", "wave_in_bar"])
+def test_gold_decks(name):
+    """The reference's regression decks at every output time: exodiff
+    tolerances against the gold files, 1e-10 against the reference run."""
+    fx, rf = load("gold_" + name), load("ref_" + name)
+    p = gold_problem(fx)
+    steps, of = int(fx["num_steps"]), int(fx["output_frequency"])
+    m = E.Model(p)
+    m.begin(float(fx["final_time"]), steps, of)
+    done = 0
+    for t, s_end in enumerate(output_steps(steps, of)):
+        m.advance(s_end - done)
+        done = s_end
+        st = m.state()
+        assert exodiff_ok(st["u"], fx["gold:displacement"][t + 1], fx["tol:displacement"])
+        assert exodiff_ok(st["v"], fx["gold:velocity"][t + 1], fx["tol:velocity"])
+        assert exodiff_ok(st["F"], fx["gold:F"][t + 1], fx["tol:F"])
+        assert exodiff_ok(st["sigma"], fx["gold:sigma"][t + 1], fx["tol:sigma"])
+        compare(st, {"u": rf["u"][t], "v": rf["v"][t], "sigma": rf["sigma"][t]})
+    m.close()
+
+
+def test_jittered_cube_against_oracle_with_output_steps():
+    p = cube_problem(12, jitter=0.2, seed=21)
+    dt = 0.5 * critical_time_step(p)
+    steps = 300
+    ref = O.run_port(p, steps * dt, steps, 70, threads=8)
+    g = E.run(p, steps * dt, steps, 70)
+    compare(g, ref)
+    assert np.array_equal(g["mass"], ref["mass"])
+    assert abs(g["kinetic_energy"] - ref["kinetic_energy"]) <= 1e-9 * ref["kinetic_energy"]
+    assert abs(g["internal_energy"] - ref["internal_energy"]) <= 1e-8 * ref["internal_energy"]
+
+
+def test_prescribed_displacement_and_initial_velocity():
+    p = cube_problem(6, jitter=0.15, seed=3)
+    p.bcs = [BoundaryCondition.parse("initial_velocity nodelist_2 x 2.5"),
+             BoundaryCondition.parse("prescribed_velocity nodelist_1 x 0.0"),
+             BoundaryCondition.parse("prescribed_velocity nodelist_1 y 0.0"),
+             BoundaryCondition.parse("prescribed_displacement nodelist_1 z 1.0e-4"),
+             BoundaryCondition(BC_PRESCRIBED_DISPLACEMENT, "nodelist_2", 1, -2.0e-5)]
+    p.v_init = None
+    dt = 0.5 * critical_time_step(p)
+    ref = O.run_port(p, 150 * dt, 150, 40)
+    g = E.run(p, 150 * dt, 150, 40)
+    compare(g, ref)
+
+
+def test_advance_in_pieces_equals_one_advance():
+    p = cube_problem(8, jitter=0.2, seed=4)
+    dt = 0.5 * critical_time_step(p)
+    a = E.Model(p, graph_steps=7)
+    a.begin(90 * dt, 90, 25)
+    for k in (1, 13, 50, 26):
+        a.advance(k)
+    sa = a.state()
+    b = E.Model(p)
+    b.begin(90 * dt, 90, 25)
+    b.advance(90)
+    sb = b.state()
+    for k in ("u", "v", "a", "f_int", "F", "sigma"):
+        assert np.array_equal(sa[k], sb[k]), k
+
+
+def test_runs_are_bitwise_deterministic():
+    p = cube_problem(10, jitter=0.2, seed=8)
+    dt = 0.5 * critical_time_step(p)
+    r1 = E.run(p, 40 * dt, 40)
+    r2 = E.run(p, 40 * dt, 40)
+    for k in ("u", "v", "a", "f_int", "F", "sigma"):
+        assert np.array_equal(r1[k], r2[k]), k
+
+
+def test_host_buffer_internal_force_matches_device_path():
+    p = cube_problem(6, jitter=0.2, seed=9)
+    rng = np.random.default_rng(0)
+    u = rng.normal(0, 1e-4, size=(p.num_nodes, 3))
+    m = E.Model(p)
+    pinned = E.PinnedArray((p.num_nodes, 3))
+    pinned.array[:] = u
+    out = E.PinnedArray((p.num_nodes, 3))
+    f_host = m.ComputeInternalForceHost(pinned.array, out.array).copy()
+    m.SetVectorNodeData("displacement", u)
+    m.ComputeInternalForce()
+    assert np.array_equal(f_host, m.GetVectorNodeData("internal_force"))
+    # against the oracle's element arithmetic, assembled in element order
+    fo = np.zeros((p.num_nodes, 3))
+    for e in range(p.num_elem):
+        X, ue = p.coords[p.conn[e]], u[p.conn[e]]
+        _, _, f = O.element(X, ue, p.bulk_modulus, p.shear_modulus)
+        for c in range(8):
+            fo[p.conn[e, c]] += f[c]
+    assert rel(f_host, fo) < 1e-10
+
+
+def test_fp32_mixed_within_1e3_of_fp64():
+    p = cube_problem(16, jitter=0.2, seed=2)
+    dt = 0.5 * critical_time_step(p)
+    a = E.run(p, 500 * dt, 500, precision="fp64")
+    b = E.run(p, 500 * dt, 500, precision="fp32")
+    assert np.array_equal(a["mass"], b["mass"])
+    e = rel(b["u"], a["u"])
+    assert e < 1e-3, e
+    assert rel(b["v"], a["v"]) < 1e-2
+
+
+def test_inverted_element_is_reported():
+    """A mesh with an inverted element: the engine returns
+    NSM_ERR_BAD_JACOBIAN at setup (the reference asserts,
+    src/nimble_utils.h:1243-1255)."""
+    p = cube_problem(2)
+    c = p.conn.copy()
+    c[0] = c[0][[4, 5, 6, 7, 0, 1, 2, 3]]  # swap top and bottom faces
+    p.conn = c
+    with pytest.raises(E.EngineError) as ei:
+        E.Model(p)
+    assert ei.value.code == 3
+
+
+def test_large_deformation_reports_inversion_and_stays_usable():
+    """Displacements that turn an element inside out flag the status word; the
+    context stays usable for the next call."""
+    p = cube_problem(3)
+    m = E.Model(p)
+    u = np.zeros((p.num_nodes, 3))
+    u[p.conn[13, 6]] = [-0.8, -0.8, -0.8]  # push the centre element's (+,+,+) corner through
+    m.SetVectorNodeData("displacement", u)
+    with pytest.raises(E.EngineError) as ei:
+        m.ComputeInternalForce()
+    assert ei.value.code in (3, 4)
+    m.SetVectorNodeData("displacement", np.zeros_like(u))
+    m.ComputeInternalForce()
+    assert np.all(m.GetVectorNodeData("internal_force") == 0.0)
+
+
+def test_128_cube_first_steps_against_oracle():
+    """The benchmark mesh (128^3 jittered, 2.1M nodes): the first steps
+    against the oracle on all host cores, plus full-size invariants."""
+    import os
+    p = cube_problem(128, jitter=0.2, seed=0)
+    dt = 0.5 * critical_time_step(p)
+    steps = 4
+    run = O.PortRun(p, threads=os.cpu_count())
+    run.begin(2000 * dt, 2000, 0)
+    run.advance(steps)
+    ref = run.state()
+    m = E.Model(p)
+    assert m.GetCriticalTimeStep() == run.dt_crit
+    m.begin(2000 * dt, 2000, 0)
+    m.advance(steps)
+    g = m.state()
+    compare(g, ref)
+    m.close()

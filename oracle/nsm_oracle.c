@@ -889,3 +889,77 @@ nsm_oracle_continue(
   nsm_oracle_destroy(o);
   return rc;
 }
+
+/* Extended-precision Cauchy stress of the displacement field u at the
+ * integration points of the listed elements (long double: at least a 64-bit
+ * significand).  The same constitutive law as the reference
+ * (src/nimble_material.cc:252-310), evaluated as
+ * sigma = K/2 (J - 1/J) I + G J^{-5/3} dev(b) with b - I = H + H^T + H H^T and
+ * H = (du/dxi)(dX/dxi)^{-1}, which has no cancellation.  Not a restatement of
+ * the reference's arithmetic: it is the accuracy yardstick the reference's and
+ * the engine's FP64 stresses are both measured against. */
+void
+nsm_oracle_stress_exact(const nsm_oracle_model* m, const double* u, int num, const int* elems, double* sigma)
+{
+  build_tables();
+  for (int q = 0; q < num; q++) {
+    int         e = elems[q];
+    long double X[8][3], U[8][3];
+    for (int n = 0; n < 8; n++)
+      for (int k = 0; k < 3; k++) {
+        X[n][k] = m->coords[3 * m->conn[8 * e + n] + k];
+        U[n][k] = u[3 * m->conn[8 * e + n] + k];
+      }
+    for (int ip = 0; ip < 8; ip++) {
+      long double JX[3][3] = {{0}}, Ju[3][3] = {{0}};
+      for (int j = 0; j < 8; j++)
+        for (int i = 0; i < 3; i++)
+          for (int k = 0; k < 3; k++) {
+            JX[i][k] += X[j][i] * (long double)g_dN[24 * ip + 3 * j + k];
+            Ju[i][k] += U[j][i] * (long double)g_dN[24 * ip + 3 * j + k];
+          }
+      long double c[3][3];
+      c[0][0] = JX[1][1] * JX[2][2] - JX[1][2] * JX[2][1];
+      c[0][1] = JX[0][2] * JX[2][1] - JX[0][1] * JX[2][2];
+      c[0][2] = JX[0][1] * JX[1][2] - JX[0][2] * JX[1][1];
+      c[1][0] = JX[1][2] * JX[2][0] - JX[1][0] * JX[2][2];
+      c[1][1] = JX[0][0] * JX[2][2] - JX[0][2] * JX[2][0];
+      c[1][2] = JX[0][2] * JX[1][0] - JX[0][0] * JX[1][2];
+      c[2][0] = JX[1][0] * JX[2][1] - JX[1][1] * JX[2][0];
+      c[2][1] = JX[0][1] * JX[2][0] - JX[0][0] * JX[2][1];
+      c[2][2] = JX[0][0] * JX[1][1] - JX[0][1] * JX[1][0];
+      long double det = JX[0][0] * c[0][0] + JX[0][1] * c[1][0] + JX[0][2] * c[2][0];
+      long double H[3][3];
+      for (int i = 0; i < 3; i++)
+        for (int J = 0; J < 3; J++) {
+          long double h = 0;
+          for (int k = 0; k < 3; k++) h += Ju[i][k] * c[k][J] / det;
+          H[i][J] = h;
+        }
+      long double F[3][3];
+      for (int i = 0; i < 3; i++)
+        for (int k = 0; k < 3; k++) F[i][k] = (i == k ? 1.0L : 0.0L) + H[i][k];
+      long double Jd = F[0][0] * (F[1][1] * F[2][2] - F[1][2] * F[2][1]) -
+                       F[0][1] * (F[1][0] * F[2][2] - F[1][2] * F[2][0]) +
+                       F[0][2] * (F[1][0] * F[2][1] - F[1][1] * F[2][0]);
+      long double B[3][3];
+      for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) {
+          long double t = H[i][0] * H[j][0] + H[i][1] * H[j][1] + H[i][2] * H[j][2];
+          B[i][j]       = H[i][j] + H[j][i] + t;
+        }
+      long double r   = 1.0L / cbrtl(Jd);
+      long double pr  = 0.5L * (long double)m->bulk_modulus * (Jd - 1.0L / Jd);
+      long double mm  = (B[0][0] + B[1][1] + B[2][2]) / 3.0L;
+      long double Gr5 = (long double)m->shear_modulus * r * r * r * r * r;
+      double*     s   = &sigma[48 * (size_t)q + 6 * ip];
+      s[0]            = (double)(pr + Gr5 * (B[0][0] - mm));
+      s[1]            = (double)(pr + Gr5 * (B[1][1] - mm));
+      s[2]            = (double)(pr + Gr5 * (B[2][2] - mm));
+      s[3]            = (double)(Gr5 * B[0][1]);
+      s[4]            = (double)(Gr5 * B[1][2]);
+      s[5]            = (double)(Gr5 * B[2][0]);
+    }
+  }
+}
+

@@ -116,6 +116,10 @@ int nsm_oracle_continue(
     double*                 a,
     double*                 loop_seconds);
 
+/* Extended-precision stress of displacement u at the points of `num` listed
+ * elements -> sigma [num][8][6]: the accuracy yardstick (see nsm_oracle.c). */
+void nsm_oracle_stress_exact(const nsm_oracle_model* m, const double* u, int num, const int* elems, double* sigma);
+
 /* Stateful form of the same loop, for reading intermediate states. */
 typedef struct nsm_oracle nsm_oracle;
 nsm_oracle* nsm_oracle_create(const nsm_oracle_model* m, int num_threads); /* lumped mass, dt_crit */

@@ -95,6 +95,7 @@ def port():
         lib.nsm_oracle_get_state.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp, _dp, _dp, _dp]
         lib.nsm_oracle_set_state.argtypes = [C.c_void_p, _dp, _dp, _dp]
         lib.nsm_oracle_energies.argtypes = [C.c_void_p, _dp, _dp]
+        lib.nsm_oracle_stress_exact.argtypes = [C.POINTER(_Model), _dp, C.c_int, _ip, _dp]
         _port = lib
     return _port
 
@@ -265,6 +266,18 @@ def stress(F, K, G, which="port"):
         if ref().nimref_stress(F.shape[0], _d(F), K, G, _d(s)) != 0:
             raise RuntimeError(ref().nimref_last_error().decode())
     return s
+
+
+def stress_exact(problem, u, elems):
+    """Extended-precision stress of displacement u at the points of `elems`
+    ([len(elems), 8, 6]): the yardstick for the FP64 stresses' accuracy."""
+    keep = []
+    m = _model(problem, keep)
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    elems = np.ascontiguousarray(elems, dtype=np.int32)
+    out = np.zeros((len(elems), 8, 6))
+    port().nsm_oracle_stress_exact(C.byref(m), _d(u), len(elems), _i(elems), _d(out))
+    return out
 
 
 def shape_tables():

@@ -166,8 +166,21 @@ def ref_cube_fixture(name, n, jitter, seed, steps, output_frequency, sample_elem
         fx["F"], fx["sigma"] = r["F"][idx], r["sigma"][idx]
         fx["F_norm"] = np.linalg.norm(r["F"])
         fx["sigma_norm"] = np.linalg.norm(r["sigma"])
+        fx["sigma_elem"] = r["sigma"].mean(axis=1)  # volume-weighting aside, the element mean
+    # The reference's own sensitivity: the same run with the initial velocity
+    # perturbed by one ulp (relative 2^-52, seeded signs).  Two correct FP64
+    # codes cannot be expected to agree more closely than this.
+    q = cube_problem(n, jitter=jitter, seed=seed)
+    rng = np.random.default_rng(77)
+    q.v_init = q.v_init * (1.0 + rng.choice([-1.0, 1.0], size=q.v_init.shape) * 2.0 ** -52)
+    rq = O.run_ref(q, final_time, steps, output_frequency)
+    rel = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))
+    fx["envelope_u"], fx["envelope_v"] = rel(rq["u"], r["u"]), rel(rq["v"], r["v"])
+    fx["envelope_sigma"] = rel(rq["sigma"], r["sigma"])
+    fx["envelope_sigma_elem"] = rel(rq["sigma"].mean(axis=1), r["sigma"].mean(axis=1))
+    fx["sigma_elem_norm"] = np.linalg.norm(r["sigma"].mean(axis=1))
     np.savez_compressed(os.path.join(HERE, f"ref_{name}.npz"), **fx)
-    print("wrote", name, r["loop_seconds"], "s")
+    print("wrote", name, r["loop_seconds"], "s", {k: fx[k] for k in fx if str(k).startswith("envelope")})
 
 
 def ref_points_fixture():

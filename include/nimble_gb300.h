@@ -177,6 +177,27 @@ int nsm_set_profiling(nsm_model* model, int enable);
 int nsm_get_profile(nsm_model* model, double* element_ms_total, int* element_launches, double* node_ms_total,
                     int* node_launches);
 
+/* Stable time step of the configuration X + u for a caller that cannot
+ * allocate GPU memory (a framework that hands out all device buffers from its
+ * own pool, code running during CUDA stream capture, a loop that must not
+ * touch the allocator).  No counterpart in the reference: it is the reference's
+ * GetCriticalTimeStep computation (min over elements of the characteristic
+ * length over the bulk wave speed) without any allocation.  All pointers are
+ * caller memory the GPU can read or write: coords [N][3], displacement [N][3]
+ * (NULL = zero), conn [E][8], dt_out one double.  It runs on `stream` (a
+ * cudaStream_t; NULL = the default stream) and returns without waiting.
+ * Its scratch is a fixed array inside this library sized for
+ * NSM_NOALLOC_MAX_ELEMENTS elements (8 MiB per GPU, held until the process
+ * exits); larger meshes are rejected with NSM_ERR_INVALID_ARGUMENT.  The first
+ * call on a device looks up the array's device address; make that first call
+ * before any stream capture.  Calls share the array: calls that overlap on the
+ * GPU (different streams or threads) race and must be serialised by the
+ * caller. */
+#define NSM_NOALLOC_MAX_ELEMENTS 1048576
+int nsm_critical_time_step_noalloc(int num_nodes, int num_elem, const double* coords, const double* displacement,
+                                   const int* conn, double density, double bulk_modulus, double* dt_out,
+                                   void* stream);
+
 /* Pinned host memory for the host-buffer entry points (page-locked so that the
  * copies run at full link bandwidth). */
 void* nsm_host_alloc(size_t bytes);

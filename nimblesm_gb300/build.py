@@ -1,7 +1,7 @@
 """Builds the engine's shared library for sm_103a with nvcc, in the source tree.
 
-nimblesm_gb300/csrc/*.cu -> nimblesm_gb300/_lib/libnimble_gb300.so.  The node
-and setup kernels are compiled with --fmad=false (their sums and products
+nimblesm_gb300/csrc/*.cu -> nimblesm_gb300/_lib/libnimble_gb300.so.  The node,
+setup and no-allocation time-step kernels are compiled with --fmad=false (their sums and products
 round as the reference's host code does); the element kernels keep FMA
 contraction.  Translation units compile in parallel; only changed ones are
 rebuilt.
@@ -20,7 +20,7 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off", "-I" + INCLUDE]
-NO_FMAD = {"node_kernels.cu", "setup_kernels.cu"}
+NO_FMAD = {"node_kernels.cu", "setup_kernels.cu", "noalloc_dt.cu"}
 
 
 def _sources():

@@ -79,6 +79,8 @@ SIGNATURES = {
     "nsm_launches_per_advance": (C.c_int, [_vp, C.c_int]),
     "nsm_set_profiling": (C.c_int, [_vp, C.c_int]),
     "nsm_get_profile": (C.c_int, [_vp, _dp, _ip, _dp, _ip]),
+    "nsm_critical_time_step_noalloc": (C.c_int, [C.c_int, C.c_int, _vp, _vp, _vp, C.c_double, C.c_double, _vp,
+                                                _vp]),
     "nsm_host_alloc": (_vp, [C.c_size_t]),
     "nsm_host_free": (None, [_vp]),
 }

@@ -1,0 +1,59 @@
+"""nsm_critical_time_step_noalloc -- the stable time step for callers that
+cannot allocate GPU memory (for example a framework that owns every device
+buffer through its own pool, or code running during CUDA stream capture).  It
+keeps its scratch in a fixed array inside the library, so the caller only
+passes the mesh, the displacement and a one-double output.
+
+Checked through the C ABI against the existing entry point
+(nsm_critical_time_step) on two calls in a row, bitwise as the other
+time-step tests are.  Collected last so that a failure here stops a -x run
+only after every other test has run.  The test allocates its own buffers
+with torch (the test is not the caller that cannot allocate)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def test_noalloc_time_step_matches_existing_entry_point():
+    torch = pytest.importorskip("torch")
+    from nimblesm_gb300 import build as B
+    from nimblesm_gb300 import engine as E
+    from nimblesm_gb300.mesh import characteristic_lengths, cube_problem
+
+    B.build()
+    lib = E.library()
+    p = cube_problem(20, jitter=0.2, seed=3)
+    model = E.Model(p)
+    dt_ref = model.GetCriticalTimeStep()
+    model.close()
+
+    dev = torch.device("cuda:0")
+    X = torch.from_numpy(np.ascontiguousarray(p.coords, dtype=np.float64)).to(dev)
+    conn = torch.from_numpy(np.ascontiguousarray(p.conn, dtype=np.int32)).to(dev)
+    out = torch.empty(1, dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream(dev).cuda_stream
+
+    for _ in range(2):  # two calls in a row: the shared scratch keeps the last call's contents
+        out.fill_(-1.0)
+        rc = lib.nsm_critical_time_step_noalloc(p.num_nodes, p.num_elem, X.data_ptr(), None, conn.data_ptr(),
+                                                p.density, p.bulk_modulus, out.data_ptr(), stream)
+        assert rc == 0, lib.nsm_last_error()
+        torch.cuda.synchronize(dev)
+        assert out.item() == dt_ref
+
+    # a displaced configuration, against the same formula evaluated on the host
+    rng = np.random.default_rng(1)
+    u = rng.uniform(-0.05, 0.05, size=p.coords.shape) / 20
+    U = torch.from_numpy(u).to(dev)
+    expect = float((characteristic_lengths(p.coords + u, p.conn) / np.sqrt(p.bulk_modulus / p.density)).min())
+    rc = lib.nsm_critical_time_step_noalloc(p.num_nodes, p.num_elem, X.data_ptr(), U.data_ptr(), conn.data_ptr(),
+                                            p.density, p.bulk_modulus, out.data_ptr(), stream)
+    assert rc == 0
+    torch.cuda.synchronize(dev)
+    assert out.item() == expect
+
+    # meshes beyond the fixed scratch are refused before anything runs
+    rc = lib.nsm_critical_time_step_noalloc(p.num_nodes, 1048576 + 1, X.data_ptr(), None, conn.data_ptr(),
+                                            p.density, p.bulk_modulus, out.data_ptr(), stream)
+    assert rc == 1

@@ -7,6 +7,28 @@
 
 namespace nsm {
 
+// Vector stores of a thread's contiguous values (16-byte aligned).
+__device__ __forceinline__ void store_vec(float* dst, const float* v, int n)
+{
+#pragma unroll
+  for (int k = 0; k < n; k += 4)
+    *reinterpret_cast<float4*>(dst + k) = make_float4(v[k], v[k + 1], v[k + 2], v[k + 3]);
+}
+__device__ __forceinline__ void store_vec(double* dst, const double* v, int n)
+{
+#pragma unroll
+  for (int k = 0; k < n; k += 2) *reinterpret_cast<double2*>(dst + k) = make_double2(v[k], v[k + 1]);
+}
+
+// Nodal values of the element: FP64 form from the FP64 field, FP32 form from
+// the FP32 copy (no FP64 conversions, which would run on the FP64 pipe).
+template <typename T>
+__device__ __forceinline__ T load_node(const double* f64, const float* f32, long i);
+template <>
+__device__ __forceinline__ double load_node<double>(const double* f64, const float*, long i) { return __ldg(&f64[i]); }
+template <>
+__device__ __forceinline__ float load_node<float>(const double*, const float* f32, long i) { return __ldg(&f32[i]); }
+
 // FP64 form: reference geometry precomputed (geo planes).  FP32 form: the
 // reference Jacobian is rebuilt from X each step with the same transform.
 template <typename T, bool kPrecomputedGeo>
@@ -27,7 +49,7 @@ __global__ void __launch_bounds__(128) k_element(ElementArgs a)
 #pragma unroll
     for (int n = 0; n < 8; n++)
 #pragma unroll
-      for (int k = 0; k < 3; k++) x[n][k] = T(__ldg(&a.u[k * ld_n + id[n]]));
+      for (int k = 0; k < 3; k++) x[n][k] = load_node<T>(a.u, a.uf, k * ld_n + id[n]);
     nodal_gradient<T>(x, Gu);
   }
   T GX[3][3][2][2];
@@ -36,7 +58,7 @@ __global__ void __launch_bounds__(128) k_element(ElementArgs a)
 #pragma unroll
     for (int n = 0; n < 8; n++)
 #pragma unroll
-      for (int k = 0; k < 3; k++) x[n][k] = T(__ldg(&a.X[k * ld_n + id[n]]));
+      for (int k = 0; k < 3; k++) x[n][k] = __ldg(&a.Xf[k * ld_n + id[n]]);
     nodal_gradient<T>(x, GX);
   }
 
@@ -52,8 +74,7 @@ __global__ void __launch_bounds__(128) k_element(ElementArgs a)
 
   const T K = T(a.bulk), Gm = T(a.shear);
   bool    bad = false;
-  T*      Fo  = reinterpret_cast<T*>(a.F);
-  T*      So  = reinterpret_cast<T*>(a.sigma);
+  T*      rec = reinterpret_cast<T*>(a.ip) + (size_t)e * kIpRecord;
   const bool store = a.store_ip || (a.sched != nullptr && a.sched[*a.step_base + a.k].is_output);
 
 #pragma unroll
@@ -87,12 +108,15 @@ __global__ void __launch_bounds__(128) k_element(ElementArgs a)
     neohookean<T>(H, K, Gm, sig, C, J);
     if (!(J > T(0)) || !(det0 > T(0))) bad = true;  // inverted element
     if (store) {
+      T r[kIpRecord];
 #pragma unroll
       for (int i = 0; i < 3; i++)
 #pragma unroll
-        for (int k = 0; k < 3; k++) Fo[(p * 9 + full_slot(i, k)) * ld_e + e] = (i == k) ? T(1) + H[i][k] : H[i][k];
+        for (int k = 0; k < 3; k++) r[full_slot(i, k)] = (i == k) ? T(1) + H[i][k] : H[i][k];
 #pragma unroll
-      for (int q = 0; q < 6; q++) So[(p * 6 + q) * ld_e + e] = sig[q];
+      for (int q = 0; q < 6; q++) r[9 + q] = sig[q];
+      r[15] = T(0);
+      store_vec(rec + (size_t)p * ld_e * kIpRecord, r, kIpRecord);
     }
     // P = sigma cof(F);  Q[d][i] = det J_X sum_J G0[d][J] P[i][J]
     T P[3][3];
@@ -132,15 +156,16 @@ __global__ void __launch_bounds__(128) k_element(ElementArgs a)
         }
     }
   }
-  T*   fo     = reinterpret_cast<T*>(a.fe);
+  T    fv[24];
   bool finite = true;
 #pragma unroll
   for (int n = 0; n < 8; n++)
 #pragma unroll
     for (int i = 0; i < 3; i++) {
-      fo[(n * 3 + i) * ld_e + e] = f[n][i];
-      finite = finite && isfinite(f[n][i]);
+      fv[n * 3 + i] = f[n][i];
+      finite        = finite && isfinite(f[n][i]);
     }
+  store_vec(reinterpret_cast<T*>(a.fe) + (size_t)e * 24, fv, 24);
   if (bad || !finite) atomicOr(a.status, (bad ? NSM_STATUS_BAD_JACOBIAN : 0) | (finite ? 0 : NSM_STATUS_NONFINITE));
 }
 
@@ -240,30 +265,44 @@ cudaError_t launch_energies(int N, long ld_n, const double* mass, const double* 
   return cudaGetLastError();
 }
 
-// SoA integration-point planes src[(p*comps + c)*ld_e + e] -> reference
-// layout dst[(e*8 + p)*comps + c] (doubles).
+// Per-point records ip[(p*ld_e + e)*16 + slot] -> reference layout
+// dst[(e*8 + p)*comps + c] in doubles (F: slots 0..8, sigma: slots 9..14).
 template <typename T>
-__global__ void k_ip_to_aos(int E, long ld_e, const T* __restrict__ src, int comps, double* __restrict__ dst)
+__global__ void k_ip_to_aos(int E, long ld_e, const T* __restrict__ ip, int which, double* __restrict__ dst)
 {
-  long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  long total = (long)E * 8 * comps;
+  const int comps = which == 0 ? 9 : 6, first = which == 0 ? 0 : 9;
+  long      i     = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  long      total = (long)E * 8 * comps;
   if (i >= total) return;
   int  c = (int)(i % comps);
   long r = i / comps;
   int  p = (int)(r % 8);
   long e = r / 8;
-  dst[i] = (double)src[(p * comps + c) * ld_e + e];
+  dst[i] = (double)ip[((size_t)p * ld_e + e) * kIpRecord + first + c];
 }
 
-cudaError_t launch_ip_to_aos(int E, long ld_e, const void* src, int src_is_float, int comps, double* dst,
+cudaError_t launch_ip_to_aos(int E, long ld_e, const void* ip, int src_is_float, int which, double* dst,
                              cudaStream_t stream)
 {
-  long total = (long)E * 8 * comps;
+  long total = (long)E * 8 * (which == 0 ? 9 : 6);
   if (total == 0) return cudaSuccess;
   if (src_is_float)
-    k_ip_to_aos<float><<<grid_for(total, 256), 256, 0, stream>>>(E, ld_e, (const float*)src, comps, dst);
+    k_ip_to_aos<float><<<grid_for(total, 256), 256, 0, stream>>>(E, ld_e, (const float*)ip, which, dst);
   else
-    k_ip_to_aos<double><<<grid_for(total, 256), 256, 0, stream>>>(E, ld_e, (const double*)src, comps, dst);
+    k_ip_to_aos<double><<<grid_for(total, 256), 256, 0, stream>>>(E, ld_e, (const double*)ip, which, dst);
+  return cudaGetLastError();
+}
+
+__global__ void k_to_float(long n, const double* __restrict__ src, float* __restrict__ dst)
+{
+  long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = (float)src[i];
+}
+
+cudaError_t launch_to_float(long n, const double* src, float* dst, cudaStream_t stream)
+{
+  if (n == 0) return cudaSuccess;
+  k_to_float<<<grid_for(n, 256), 256, 0, stream>>>(n, src, dst);
   return cudaGetLastError();
 }
 

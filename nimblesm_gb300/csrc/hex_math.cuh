@@ -103,7 +103,8 @@ __device__ __forceinline__ double rcbrt_refined(double J)
   double c  = fma(e, 2.0 / 9.0, 1.0 / 3.0);
   return fma(y * e, c, y);
 }
-__device__ __forceinline__ float rcbrt_refined(float J) { return rcbrtf(J); }
+// FP32 form: J^{-1/3} = 2^{-log2(J)/3} with the hardware log2/exp2 (about 2 ulp).
+__device__ __forceinline__ float rcbrt_refined(float J) { return exp2f(__log2f(J) * (-1.0f / 3.0f)); }
 
 // Neo-Hookean Cauchy stress from H = F - I (reference src/nimble_material.cc:252-310):
 // sigma = K/2 (J - 1/J) I + G J^{-5/3} dev(F F^T).  Also returns cof(F) and J.
@@ -155,6 +156,9 @@ __device__ __forceinline__ T sym(const T s[6], int i, int k)
   return s[sym_slot(i, k)];
 }
 
+__device__ __forceinline__ double reciprocal(double x) { return 1.0 / x; }
+__device__ __forceinline__ float  reciprocal(float x) { return __frcp_rn(x); }
+
 template <typename T>
 __device__ __forceinline__ void invert3(const T A[3][3], T inv[3][3], T& det)
 {
@@ -162,7 +166,7 @@ __device__ __forceinline__ void invert3(const T A[3][3], T inv[3][3], T& det)
   T c01 = A[1][2] * A[2][0] - A[1][0] * A[2][2];
   T c02 = A[1][0] * A[2][1] - A[1][1] * A[2][0];
   det   = A[0][0] * c00 + A[0][1] * c01 + A[0][2] * c02;
-  T r   = T(1) / det;
+  T r   = reciprocal(det);
   inv[0][0] = c00 * r;
   inv[1][0] = c01 * r;
   inv[2][0] = c02 * r;

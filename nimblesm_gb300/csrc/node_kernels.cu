@@ -43,7 +43,7 @@ __global__ void __launch_bounds__(256) k_node_update(NodeArgs a)
       const long e  = ec >> 3;
       const int  c  = ec & 7;
 #pragma unroll
-      for (int i = 0; i < 3; i++) f[i] += (double)__ldg(&fe[(c * 3 + i) * a.ld_e + e]);
+      for (int i = 0; i < 3; i++) f[i] += (double)__ldg(&fe[e * 24 + c * 3 + i]);
     }
 #pragma unroll
     for (int i = 0; i < 3; i++) a.f_int[i * ld + n] = f[i];
@@ -82,6 +82,7 @@ __global__ void __launch_bounds__(256) k_node_update(NodeArgs a)
     a.u[i * ld + n] = u[i];
     a.v[i * ld + n] = v[i];
     if (a.k_post >= 0) a.a[i * ld + n] = acc[i];
+    if (a.uf != nullptr) a.uf[i * ld + n] = (float)u[i];
   }
 }
 

@@ -34,18 +34,25 @@ void        shape_tables(double* N, double* dN);
 cudaError_t upload_shape_tables(cudaStream_t stream);
 cudaError_t launch_setup(const SetupArgs& a, cudaStream_t stream);
 
+// Per-point record of the element data: 16 values of type T per element and
+// integration point, records laid out [ip][ld_e][16]: slots 0..8 F in the
+// reference full-tensor order, 9..14 sigma in the symmetric order, 15 unused.
+// One thread writes its 64 (FP32) or 128 (FP64) contiguous bytes with vector
+// stores; a warp writes 2 or 4 KB contiguous.
+constexpr int kIpRecord = 16;
+
 // Element kernel arguments (one launch = all elements of a block).
 struct ElementArgs {
   int           E;
   long          ld_e, ld_n;
   const int*    conn;      // [8][ld_e]
-  const double* u;         // [3][ld_n] displacement
-  const double* X;         // [3][ld_n] reference coordinates (FP32 form only)
+  const double* u;         // [3][ld_n] displacement (FP64 form)
+  const float*  uf;        // [3][ld_n] FP32 copy of u (FP32 form)
+  const float*  Xf;        // [3][ld_n] FP32 copy of X (FP32 form)
   const double* geo;       // [80][ld_e] G0 and det J0 per ip (FP64 form only)
   double        bulk, shear;
-  void*         F;         // [72][ld_e] deformation gradient per ip, reference slot order (T)
-  void*         sigma;     // [48][ld_e] Cauchy stress per ip (T)
-  void*         fe;        // [24][ld_e] element nodal forces, corner-major (T)
+  void*         ip;        // [8][ld_e][16] per-point records (T)
+  void*         fe;        // [ld_e][24] element nodal forces, corner-major (T)
   int               store_ip;   // 1: write F and sigma; 0: only on output steps of the schedule
   const StepSched*  sched;      // schedule (nullable: outside the time loop)
   const int*        step_base;  // device step counter
@@ -77,6 +84,7 @@ struct NodeArgs {
   double*           v;
   double*           a;
   double*           f_int;
+  float*            uf;       // FP32 copy of u kept in step (FP32 form), or null
 };
 
 cudaError_t launch_node_update(const NodeArgs& a, cudaStream_t stream);
@@ -95,8 +103,10 @@ cudaError_t   launch_energies(int N, long ld_n, const double* mass, const double
                               double* partial, double* out, cudaStream_t stream);
 
 // Reference-layout views of SoA data ([E][8][9] / [E][8][6] / [N][3]).
-cudaError_t launch_ip_to_aos(int E, long ld_e, const void* src, int src_is_float, int comps, double* dst,
+// which: 0 = F ([E][8][9]), 1 = sigma ([E][8][6]).
+cudaError_t launch_ip_to_aos(int E, long ld_e, const void* ip, int src_is_float, int which, double* dst,
                              cudaStream_t stream);
+cudaError_t launch_to_float(long n, const double* src, float* dst, cudaStream_t stream);
 cudaError_t launch_node_soa_to_aos(int N, long ld_n, const double* src, double* dst, cudaStream_t stream);
 cudaError_t launch_node_aos_to_soa(int N, long ld_n, const double* src, double* dst, cudaStream_t stream);
 

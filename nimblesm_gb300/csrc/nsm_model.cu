@@ -66,9 +66,10 @@ struct nsm_model {
   double* d_mass = nullptr;
   double* d_inv_mass = nullptr;
   double* d_geo = nullptr;  // [80][ld_e]
-  void*   d_F = nullptr;    // [72][ld_e]
-  void*   d_sigma = nullptr;// [48][ld_e]
-  void*   d_fe = nullptr;   // [24][ld_e]
+  void*   d_ip = nullptr;   // [8][ld_e][16] per-point F and sigma records
+  void*   d_fe = nullptr;   // [ld_e][24] element nodal forces
+  float*  d_Xf = nullptr;   // FP32 copies of X and u (FP32 form)
+  float*  d_uf = nullptr;
   int*    d_status = nullptr;
   int*    d_step_base = nullptr;
   double* d_scratch = nullptr;  // energy partials / setup temporaries
@@ -107,8 +108,8 @@ void free_all(nsm_model* m)
   for (auto& g : m->graphs) cudaGraphExecDestroy(g.second);
   m->graphs.clear();
   void* ptrs[] = {m->d_conn, m->d_node_ptr, m->d_node_inc, m->d_X,     m->d_u,         m->d_v,     m->d_a,
-                  m->d_f,    m->d_fext,     m->d_mass,     m->d_inv_mass, m->d_geo,    m->d_F,     m->d_sigma,
-                  m->d_fe,   m->d_status,   m->d_step_base, m->d_scratch, m->d_stage,  m->d_out,   m->d_bc_slot,
+                  m->d_f,    m->d_fext,     m->d_mass,     m->d_inv_mass, m->d_geo,    m->d_ip,    m->d_Xf,
+                  m->d_uf,   m->d_fe,   m->d_status,   m->d_step_base, m->d_scratch, m->d_stage,  m->d_out,   m->d_bc_slot,
                   m->d_bcs,  m->d_ibc_slot, m->d_ibcs,     m->d_sched};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -196,12 +197,12 @@ nsm::ElementArgs element_args(nsm_model* m, int k)
   a.ld_n      = m->ld_n;
   a.conn      = m->d_conn;
   a.u         = m->d_u;
-  a.X         = m->d_X;
+  a.uf        = m->d_uf;
+  a.Xf        = m->d_Xf;
   a.geo       = m->d_geo;
   a.bulk      = m->K;
   a.shear     = m->G;
-  a.F         = m->d_F;
-  a.sigma     = m->d_sigma;
+  a.ip        = m->d_ip;
   a.fe        = m->d_fe;
   a.store_ip  = (k < 0 || m->store_ip) ? 1 : 0;
   a.sched     = k < 0 ? nullptr : m->d_sched;
@@ -233,7 +234,16 @@ nsm::NodeArgs node_args(nsm_model* m, int k_post, int k_pre, int gather_only)
   a.v           = m->d_v;
   a.a           = m->d_a;
   a.f_int       = m->d_f;
+  a.uf          = m->d_uf;
   return a;
+}
+
+// The FP32 form reads an FP32 copy of u; refresh it after u is written from
+// outside the node kernel.
+cudaError_t sync_uf(nsm_model* m)
+{
+  if (!m->d_uf) return cudaSuccess;
+  return nsm::launch_to_float(3 * m->ld_n, m->d_u, m->d_uf, m->stream);
 }
 
 cudaError_t launch_element(nsm_model* m, int k)
@@ -366,12 +376,15 @@ int nsm_create(const nsm_mesh_desc* mesh, const nsm_neohookean* material, const 
   NSM_CUDA_B(cudaMalloc(&m->d_mass, sizeof(double) * m->ld_n));
   NSM_CUDA_B(cudaMalloc(&m->d_inv_mass, sizeof(double) * m->ld_n));
   NSM_CUDA_B(cudaMalloc(&m->d_geo, sizeof(double) * 80 * m->ld_e));
-  NSM_CUDA_B(cudaMalloc(&m->d_F, eb * 72 * m->ld_e));
-  NSM_CUDA_B(cudaMalloc(&m->d_sigma, eb * 48 * m->ld_e));
+  NSM_CUDA_B(cudaMalloc(&m->d_ip, eb * nsm::kIpRecord * 8 * m->ld_e));
   NSM_CUDA_B(cudaMalloc(&m->d_fe, eb * 24 * m->ld_e));
-  NSM_CUDA_B(cudaMemsetAsync(m->d_F, 0, eb * 72 * m->ld_e, m->stream));
-  NSM_CUDA_B(cudaMemsetAsync(m->d_sigma, 0, eb * 48 * m->ld_e, m->stream));
+  NSM_CUDA_B(cudaMemsetAsync(m->d_ip, 0, eb * nsm::kIpRecord * 8 * m->ld_e, m->stream));
   NSM_CUDA_B(cudaMemsetAsync(m->d_fe, 0, eb * 24 * m->ld_e, m->stream));
+  if (m->precision == NSM_PRECISION_FP32_MIXED) {
+    NSM_CUDA_B(cudaMalloc(&m->d_Xf, sizeof(float) * 3 * m->ld_n));
+    NSM_CUDA_B(cudaMalloc(&m->d_uf, sizeof(float) * 3 * m->ld_n));
+    NSM_CUDA_B(cudaMemsetAsync(m->d_uf, 0, sizeof(float) * 3 * m->ld_n, m->stream));
+  }
   NSM_CUDA_B(cudaMalloc(&m->d_status, sizeof(int)));
   NSM_CUDA_B(cudaMemsetAsync(m->d_status, 0, sizeof(int), m->stream));
   NSM_CUDA_B(cudaMalloc(&m->d_step_base, sizeof(int)));
@@ -399,6 +412,7 @@ int nsm_create(const nsm_mesh_desc* mesh, const nsm_neohookean* material, const 
     NSM_CUDA_B(cudaMemcpyAsync(m->d_conn, conn_soa.data(), sizeof(int) * conn_soa.size(), cudaMemcpyHostToDevice,
                                m->stream));
     NSM_CUDA_B(cudaMemcpyAsync(m->d_X, X.data(), sizeof(double) * X.size(), cudaMemcpyHostToDevice, m->stream));
+    if (m->d_Xf) NSM_CUDA_B(nsm::launch_to_float(3 * m->ld_n, m->d_X, m->d_Xf, m->stream));
     NSM_CUDA_B(cudaMemcpyAsync(m->d_node_ptr, ptr.data(), sizeof(int) * ptr.size(), cudaMemcpyHostToDevice,
                                m->stream));
     if (E > 0)
@@ -518,6 +532,7 @@ int nsm_set_node_field(nsm_model* m, int field, const double* values)
   if (m->N == 0) return NSM_OK;
   NSM_CUDA(cudaMemcpyAsync(m->d_stage, values, sizeof(double) * 3 * m->N, cudaMemcpyHostToDevice, m->stream));
   NSM_CUDA(nsm::launch_node_aos_to_soa(m->N, m->ld_n, m->d_stage, dst, m->stream));
+  if (dst == m->d_u) NSM_CUDA(sync_uf(m));
   NSM_CUDA(cudaStreamSynchronize(m->stream));
   return NSM_OK;
 }
@@ -552,6 +567,7 @@ int nsm_compute_internal_force_host(nsm_model* m, const double* displacement, do
   const size_t bytes = sizeof(double) * 3 * m->N;
   NSM_CUDA(cudaMemcpyAsync(m->d_stage, displacement, bytes, cudaMemcpyHostToDevice, m->stream));
   NSM_CUDA(nsm::launch_node_aos_to_soa(m->N, m->ld_n, m->d_stage, m->d_u, m->stream));
+  NSM_CUDA(sync_uf(m));
   NSM_CUDA(launch_element(m, -1));
   NSM_CUDA(nsm::launch_node_update(node_args(m, -1, -1, 1), m->stream));
   NSM_CUDA(nsm::launch_node_soa_to_aos(m->N, m->ld_n, m->d_f, m->d_stage, m->stream));
@@ -569,13 +585,13 @@ int nsm_get_ip_data(nsm_model* m, double* F, double* sigma)
   NSM_CUDA(cudaMalloc(&tmp, sizeof(double) * 72 * (size_t)m->E));
   cudaError_t e = cudaSuccess;
   if (F) {
-    e = nsm::launch_ip_to_aos(m->E, m->ld_e, m->d_F, is_float, 9, tmp, m->stream);
+    e = nsm::launch_ip_to_aos(m->E, m->ld_e, m->d_ip, is_float, 0, tmp, m->stream);
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(F, tmp, sizeof(double) * 72 * (size_t)m->E, cudaMemcpyDeviceToHost, m->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(m->stream);
   }
   if (sigma && e == cudaSuccess) {
-    e = nsm::launch_ip_to_aos(m->E, m->ld_e, m->d_sigma, is_float, 6, tmp, m->stream);
+    e = nsm::launch_ip_to_aos(m->E, m->ld_e, m->d_ip, is_float, 1, tmp, m->stream);
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(sigma, tmp, sizeof(double) * 48 * (size_t)m->E, cudaMemcpyDeviceToHost, m->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(m->stream);
@@ -631,6 +647,7 @@ int nsm_begin(nsm_model* m, double initial_time, double final_time, int num_step
   NSM_CUDA(cudaMemsetAsync(m->d_step_base, 0, sizeof(int), m->stream));
   const size_t nb = sizeof(double) * 3 * m->ld_n;
   NSM_CUDA(cudaMemsetAsync(m->d_u, 0, nb, m->stream));
+  NSM_CUDA(sync_uf(m));
   NSM_CUDA(cudaMemsetAsync(m->d_v, 0, nb, m->stream));
   NSM_CUDA(cudaMemsetAsync(m->d_a, 0, nb, m->stream));
   NSM_CUDA(cudaMemsetAsync(m->d_f, 0, nb, m->stream));

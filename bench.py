@@ -32,7 +32,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-from nimblesm_gb300.mesh import cube_problem, critical_time_step  # noqa: E402
+from nimblesm_gb300.mesh import cube_problem, critical_time_step, uq_ensemble  # noqa: E402
 
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
@@ -163,7 +163,7 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * secs / steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"hex8 neo-Hookean explicit step, jittered {n}^3 cube (config 1)",
+        "config": {"workload": f"hex8 neo-Hookean explicit step, jittered {n}^3 cube (±20% interior jitter), dt = 0.5 dt_crit",
                    "elements": problem.num_elem, "nodes": problem.num_nodes, "steps_requested": args.steps},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{steps} full steps of the {n}^3 mesh"},
@@ -171,6 +171,37 @@ def run_reference(args):
     }
     print(json.dumps(line), flush=True)
     return 0
+
+
+def uq_variants(E, args, device):
+    """Ensemble workload: 512 jittered cubes with n ~ U{8..48} and log-normal moduli in
+    one handle (one launch per phase for all samples), each sample with its
+    own time step, CUDA graphs of 100 steps; launch shape by the autotuner.
+    QoI per sample: max |u_z| on its z = L face."""
+    probs = uq_ensemble(num_samples=args.uq_samples, seed=0)
+    E_tot = sum(p.num_elem for p in probs)
+    out = {}
+    for precision in ("fp64", "fp32"):
+        m = E.Model(probs, precision=precision, graph_steps=100, device=device)
+        dts = m.sample_time_steps()
+        schedule = max(1000, args.uq_steps + 200)
+        m.begin([schedule * 0.5 * d for d in dts], schedule, schedule)
+        choice, tune_ms = m.autotune(repeats=3)
+        m.advance(100)  # warm-up chunk (graph capture)
+        m.synchronize()
+        with ClockSampler(device) as clk:
+            ms = m.advance_timed(args.uq_steps)
+        top = [p.node_sets["nodelist_2"] for p in probs]
+        q = m.sample_max_abs("displacement", 2, top)
+        out[f"uq_ensemble_{precision}"] = {
+            "value": 8.0 * E_tot * args.uq_steps / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms / args.uq_steps,
+            "samples": len(probs), "elements": E_tot, "nodes": int(sum(p.num_nodes for p in probs)),
+            "steps_timed": args.uq_steps, "after_steps": 100 + args.uq_steps, "graph_steps": 100,
+            "autotune_choice": choice, "element_launch_ms_tuned": tune_ms,
+            "qoi_max_abs_uz": {"min": float(q.min()), "mean": float(q.mean()), "max": float(q.max())},
+            "clocks": clk.summary()}
+        m.close()
+    return out
 
 
 def run_ours(args):
@@ -262,7 +293,7 @@ def run_ours(args):
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
         "data": "synthetic",
-        "config": {"workload": f"hex8 neo-Hookean explicit step, jittered {n}^3 cube (config 1), "
+        "config": {"workload": f"hex8 neo-Hookean explicit step, jittered {n}^3 cube (±20% interior jitter), dt = 0.5 dt_crit, "
                                f"{args.precision}", "elements": E_, "nodes": N, "ips_per_step": 8 * E_,
                    "dt": dt, "schedule_steps": sched, "parallelism": f"replicas{ws}",
                    "l2": "inputs larger than L2 (per-step traffic >> 129 MB)"},
@@ -285,6 +316,8 @@ def run_ours(args):
                           "rel_disp_err_vs_fp64": err, "after_steps": args.warmup + args.steps,
                           "element_launch_ms": r["prof"]["element_ms"] / max(r["prof"]["element_launches"], 1),
                           "clocks": r["clocks"]}
+    if args.uq_steps > 0:
+        variants.update(uq_variants(E, args, local if ws > 1 else 0))
     if variants:
         line["variants"] = variants
     if rank == 0 and not args.no_cpu_baseline:
@@ -303,10 +336,12 @@ def main():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
-    ap.add_argument("--n", type=int, default=128, help="cube divisions (default 128: config 1)")
+    ap.add_argument("--n", type=int, default=128, help="cube divisions (default 128: 2,097,152 elements)")
     ap.add_argument("--precision", choices=("fp64", "fp32"), default="fp64")
     ap.add_argument("--no-variants", dest="variants", action="store_false")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--uq-steps", type=int, default=100, help="timed steps of the 512-sample ensemble (0: skip)")
+    ap.add_argument("--uq-samples", type=int, default=512)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

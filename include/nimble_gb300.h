@@ -98,6 +98,23 @@ int nsm_create(const nsm_mesh_desc* mesh, const nsm_neohookean* material, const 
                nsm_model** out);
 int nsm_destroy(nsm_model* model);
 
+/* Ensemble of independent samples in one handle (uncertainty quantification:
+ * meshes of uneven size and per-sample material).  The samples' meshes are
+ * concatenated: sample g's nodes and elements get global ids offset by
+ * node_offsets[g] / elem_offsets[g] (nsm_ensemble_offsets), and every entry
+ * point below works on the whole ensemble at once, each sample with its own
+ * material and time schedule.  Each sample computes exactly what
+ * nsm_create on its mesh alone computes.  The reference runs such samples one
+ * at a time (one process per sample; its UQ mode, src/uq/nimble_uq_model_data.cc:145-248,
+ * shares one mesh).  meshes, materials: [num_samples]. */
+int nsm_create_ensemble(int num_samples, const nsm_mesh_desc* meshes, const nsm_neohookean* materials,
+                        const nsm_options* options, nsm_model** out);
+int nsm_ensemble_offsets(nsm_model* model, int* node_offsets, int* elem_offsets); /* [S+1] each */
+int nsm_ensemble_time_steps(nsm_model* model, double* dt);                      /* [S] critical steps */
+/* Per-sample max |field component| over the listed (global) node ids, out [S]
+ * (e.g. max |u_z| on each sample's top face). */
+int nsm_ensemble_max_abs(nsm_model* model, int field, int component, const int* nodes, int count, double* out);
+
 /* One boundary-condition line "<kind> <nodeset> <x|y|z> <value>" over a node
  * list, in deck order (BoundaryConditionManager::Initialize,
  * src/nimble_boundary_condition_manager.cc:52-72).  component 0..2. */
@@ -153,6 +170,10 @@ int nsm_get_energies(nsm_model* model, double* kinetic, double* internal);
 int nsm_begin(nsm_model* model, double initial_time, double final_time, int num_steps, int output_frequency,
               const double* v_init);
 int nsm_advance(nsm_model* model, int num_steps);
+/* nsm_begin for an ensemble: sample g runs num_steps steps of
+ * dt_g = (final_times[g] - initial_time) / num_steps. */
+int nsm_begin_ensemble(nsm_model* model, double initial_time, const double* final_times, int num_steps,
+                       int output_frequency, const double* v_init);
 /* nsm_advance bracketed by CUDA events on the handle's stream; waits for the
  * steps and returns their device time in milliseconds. */
 int nsm_advance_timed(nsm_model* model, int num_steps, double* device_ms);
@@ -168,6 +189,11 @@ int nsm_check_status(nsm_model* model);
  * handle's stream) of `repeats` launches of the element kernel alone and of
  * the node kernel alone, in milliseconds. */
 int nsm_time_kernels(nsm_model* model, int repeats, double* element_ms, double* node_ms);
+/* Picks the element kernel's launch shape (elements per block; one pass or a
+ * persistent grid walking all samples' elements) by timing `repeats`
+ * launches of each candidate on this model; returns the chosen candidate and
+ * its mean time in milliseconds.  Captured graphs are rebuilt. */
+int nsm_autotune(nsm_model* model, int repeats, int* chosen, double* best_ms);
 /* Number of kernel launches nsm_advance(model, num_steps) issues. */
 int nsm_launches_per_advance(nsm_model* model, int num_steps);
 /* Profiling mode: nsm_advance launches without CUDA graphs and brackets each

@@ -32,10 +32,25 @@ __device__ __forceinline__ float load_node<float>(const double*, const float* f3
 // FP64 form: reference geometry precomputed (geo planes).  FP32 form: the
 // reference Jacobian is rebuilt from X each step with the same transform.
 template <typename T, bool kPrecomputedGeo>
+__device__ __forceinline__ void element_work(const ElementArgs& a, const int e);
+
+// One thread per element, or (persistent form) a fixed grid of blocks walking
+// the elements of all samples in tiles of blockDim.x.
+template <typename T, bool kPrecomputedGeo, bool kPersistent>
 __global__ void __launch_bounds__(128) k_element(ElementArgs a)
 {
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= a.E) return;
+  if (!kPersistent) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < a.E) element_work<T, kPrecomputedGeo>(a, e);
+    return;
+  }
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < a.E; e += (long)gridDim.x * blockDim.x)
+    element_work<T, kPrecomputedGeo>(a, (int)e);
+}
+
+template <typename T, bool kPrecomputedGeo>
+__device__ __forceinline__ void element_work(const ElementArgs& a, const int e)
+{
   const long ld_e = a.ld_e, ld_n = a.ld_n;
 
   int id[8];
@@ -72,10 +87,16 @@ __global__ void __launch_bounds__(128) k_element(ElementArgs a)
 #pragma unroll
         for (int t = 0; t < 2; t++) S[d][i][s][t] = T(0);
 
-  const T K = T(a.bulk), Gm = T(a.shear);
+  T K = T(a.bulk), Gm = T(a.shear);
+  if (a.elem_group) {
+    const GroupMaterial& m = a.mats[__ldg(&a.elem_group[e])];
+    K                      = T(m.bulk);
+    Gm                     = T(m.shear);
+  }
   bool    bad = false;
   T*      rec = reinterpret_cast<T*>(a.ip) + (size_t)e * kIpRecord;
-  const bool store = a.store_ip || (a.sched != nullptr && a.sched[*a.step_base + a.k].is_output);
+  const bool store =
+      a.store_ip || (a.sched != nullptr && a.sched[(long)(*a.step_base + a.k) * a.num_groups].is_output);
 
 #pragma unroll
   for (int p = 0; p < 8; p++) {
@@ -169,18 +190,44 @@ __global__ void __launch_bounds__(128) k_element(ElementArgs a)
   if (bad || !finite) atomicOr(a.status, (bad ? NSM_STATUS_BAD_JACOBIAN : 0) | (finite ? 0 : NSM_STATUS_NONFINITE));
 }
 
-cudaError_t launch_element_fp64(const ElementArgs& a, cudaStream_t stream)
+int num_sms()
+{
+  static int n = 0;
+  if (n == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (n <= 0) n = 1;
+  }
+  return n;
+}
+
+template <typename T, bool kGeo>
+static cudaError_t launch_element(ElementArgs a, const ElementLaunch& l, cudaStream_t stream)
 {
   if (a.E == 0) return cudaSuccess;
-  k_element<double, true><<<grid_for(a.E, 128), 128, 0, stream>>>(a);
+  const int block = (l.block == 64 || l.block == 128) ? l.block : 128;
+  a.persistent    = l.persistent;
+  int grid        = grid_for(a.E, block);
+  if (l.persistent) {
+    int g = l.blocks_per_sm * num_sms();
+    if (g < grid) grid = g;
+  }
+  if (l.persistent)
+    k_element<T, kGeo, true><<<grid, block, 0, stream>>>(a);
+  else
+    k_element<T, kGeo, false><<<grid, block, 0, stream>>>(a);
   return cudaGetLastError();
 }
 
-cudaError_t launch_element_fp32(const ElementArgs& a, cudaStream_t stream)
+cudaError_t launch_element_fp64(const ElementArgs& a, const ElementLaunch& l, cudaStream_t stream)
 {
-  if (a.E == 0) return cudaSuccess;
-  k_element<float, false><<<grid_for(a.E, 128), 128, 0, stream>>>(a);
-  return cudaGetLastError();
+  return launch_element<double, true>(a, l, stream);
+}
+
+cudaError_t launch_element_fp32(const ElementArgs& a, const ElementLaunch& l, cudaStream_t stream)
+{
+  return launch_element<float, false>(a, l, stream);
 }
 
 // Energies of the current state, FP64 whatever the element precision:
@@ -190,7 +237,9 @@ cudaError_t launch_element_fp32(const ElementArgs& a, cudaStream_t stream)
 __global__ void __launch_bounds__(128) k_energy_partials(int N, long ld_n, const double* __restrict__ mass,
                                                          const double* __restrict__ v, int E, long ld_e,
                                                          const int* __restrict__ conn, const double* __restrict__ u,
-                                                         const double* __restrict__ geo, double K, double Gm,
+                                                         const double* __restrict__ geo,
+                                                         const int* __restrict__ elem_group,
+                                                         const GroupMaterial* __restrict__ mats,
                                                          double* __restrict__ partial)
 {
   __shared__ double s_ke[128], s_ie[128];
@@ -209,6 +258,8 @@ __global__ void __launch_bounds__(128) k_energy_partials(int N, long ld_n, const
     }
     double Gu[3][3][2][2];
     nodal_gradient<double>(x, Gu);
+    const GroupMaterial& mat = mats[elem_group ? elem_group[e] : 0];
+    const double         K = mat.bulk, Gm = mat.shear;
 #pragma unroll 1
     for (int p = 0; p < 8; p++) {
       const int bit[3] = {sx_of(p), sy_of(p), sz_of(p)};
@@ -256,11 +307,11 @@ __global__ void k_energy_final(int nblocks, const double* __restrict__ partial, 
 }
 
 cudaError_t launch_energies(int N, long ld_n, const double* mass, const double* v, int E, long ld_e,
-                            const int* conn, const double* u, const double* geo, double bulk, double shear,
-                            double* partial, double* out, cudaStream_t stream)
+                            const int* conn, const double* u, const double* geo, const int* elem_group,
+                            const GroupMaterial* mats, double* partial, double* out, cudaStream_t stream)
 {
   const int blocks = kEnergyBlocks;
-  k_energy_partials<<<blocks, 128, 0, stream>>>(N, ld_n, mass, v, E, ld_e, conn, u, geo, bulk, shear, partial);
+  k_energy_partials<<<blocks, 128, 0, stream>>>(N, ld_n, mass, v, E, ld_e, conn, u, geo, elem_group, mats, partial);
   k_energy_final<<<1, 32, 0, stream>>>(blocks, partial, out);
   return cudaGetLastError();
 }
@@ -290,6 +341,30 @@ cudaError_t launch_ip_to_aos(int E, long ld_e, const void* ip, int src_is_float,
     k_ip_to_aos<float><<<grid_for(total, 256), 256, 0, stream>>>(E, ld_e, (const float*)ip, which, dst);
   else
     k_ip_to_aos<double><<<grid_for(total, 256), 256, 0, stream>>>(E, ld_e, (const double*)ip, which, dst);
+  return cudaGetLastError();
+}
+
+// Per-sample max |x| over listed nodes; values are non-negative doubles, so
+// their bit patterns order like 64-bit integers and atomicMax on the bits is
+// an exact, order-independent maximum.
+__global__ void k_group_max_abs(int count, const int* __restrict__ nodes, const double* __restrict__ field, long ld_n,
+                                int component, const int* __restrict__ node_group, unsigned long long* out)
+{
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  int    n = nodes[i];
+  double v = fabs(field[component * ld_n + n]);
+  int    g = node_group ? node_group[n] : 0;
+  atomicMax(&out[g], (unsigned long long)__double_as_longlong(v));
+}
+
+cudaError_t launch_group_max_abs(int count, const int* nodes, const double* field, long ld_n, int component,
+                                 const int* node_group, int num_groups, double* out, cudaStream_t stream)
+{
+  cudaError_t e = cudaMemsetAsync(out, 0, sizeof(double) * num_groups, stream);
+  if (e != cudaSuccess || count == 0) return e;
+  k_group_max_abs<<<grid_for(count, 256), 256, 0, stream>>>(count, nodes, field, ld_n, component, node_group,
+                                                            reinterpret_cast<unsigned long long*>(out));
   return cudaGetLastError();
 }
 

@@ -28,7 +28,8 @@ __global__ void __launch_bounds__(256) k_node_update(NodeArgs a)
   if (n >= a.N) return;
   const long ld = a.ld_n;
   double     u[3], v[3], acc[3];
-  const int  slot = a.bc_slot[n];
+  const int  slot  = a.bc_slot[n];
+  const int  group = a.node_group ? __ldg(&a.node_group[n]) : 0;
   NodeBC     bc;
   if (slot >= 0) bc = a.bcs[slot];
 
@@ -48,7 +49,7 @@ __global__ void __launch_bounds__(256) k_node_update(NodeArgs a)
 #pragma unroll
     for (int i = 0; i < 3; i++) a.f_int[i * ld + n] = f[i];
     if (a.gather_only) return;
-    const StepSched s  = a.sched[*a.step_base + a.k_post];
+    const StepSched s  = a.sched[(long)(*a.step_base + a.k_post) * a.num_groups + group];
     const double    im = a.inv_mass[n];
 #pragma unroll
     for (int i = 0; i < 3; i++) {
@@ -69,7 +70,7 @@ __global__ void __launch_bounds__(256) k_node_update(NodeArgs a)
   if (a.k_pre >= 0) {
     // v^{n+1/2} = v^n + dt/2 a^n; BCs; u^{n+1} = u^n + dt v^{n+1/2}; BCs
     // (src/integrators/explicit_time_integrator.cc:200-223)
-    const StepSched s = a.sched[*a.step_base + a.k_pre];
+    const StepSched s = a.sched[(long)(*a.step_base + a.k_pre) * a.num_groups + group];
 #pragma unroll
     for (int i = 0; i < 3; i++) v[i] = v[i] + s.half * acc[i];
     if (slot >= 0) apply_bc(bc, s.delta, u, v);

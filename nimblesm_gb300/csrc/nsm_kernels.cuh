@@ -12,19 +12,27 @@
 
 namespace nsm {
 
+// Material of one sample of an ensemble (one entry for a single mesh).
+struct GroupMaterial {
+  double bulk, shear, density, sound_speed;
+};
+
 struct SetupArgs {
   int           N, E;
+  int           num_groups;      // samples; elements of sample g are [elem_off[g], elem_off[g+1])
+  const int*    elem_group;      // [E] sample of each element (null: one sample)
+  const int*    elem_off;        // [num_groups+1]
+  const GroupMaterial* mats;     // [num_groups]
   long          ld_n, ld_e;
   const int*    conn;      // [8][ld_e]
   const double* X;         // [3][ld_n]
   const int*    node_ptr;  // [N+1]
   const int*    node_inc;  // 8*e + corner, increasing e per node
-  double        density, sound_speed;
   double*       geo;       // [80][ld_e]
   double*       me;        // [8][ld_e]
   double*       dt_elem;   // [E]
   double*       dt_partial;// [1024]
-  double*       dt_out;    // [1]
+  double*       dt_out;    // [num_groups] per-sample critical time step
   double*       mass;      // [N]
   double*       inv_mass;  // [N]
   int*          status;
@@ -50,7 +58,11 @@ struct ElementArgs {
   const float*  uf;        // [3][ld_n] FP32 copy of u (FP32 form)
   const float*  Xf;        // [3][ld_n] FP32 copy of X (FP32 form)
   const double* geo;       // [80][ld_e] G0 and det J0 per ip (FP64 form only)
-  double        bulk, shear;
+  double        bulk, shear;     // material when elem_group is null
+  const int*    elem_group;      // [E] sample of each element, or null
+  const GroupMaterial* mats;     // [num_groups]
+  int           num_groups;
+  int           persistent;      // 0: one thread per element; 1: grid-stride over elements
   void*         ip;        // [8][ld_e][16] per-point records (T)
   void*         fe;        // [ld_e][24] element nodal forces, corner-major (T)
   int               store_ip;   // 1: write F and sigma; 0: only on output steps of the schedule
@@ -60,8 +72,15 @@ struct ElementArgs {
   int*              status;
 };
 
-cudaError_t launch_element_fp64(const ElementArgs& a, cudaStream_t stream);
-cudaError_t launch_element_fp32(const ElementArgs& a, cudaStream_t stream);
+// Launch shape of the element kernel (chosen by the autotuner).
+struct ElementLaunch {
+  int block;        // threads per block
+  int persistent;   // 0: one thread per element, 1: grid-stride with `waves` blocks per SM
+  int blocks_per_sm;
+};
+cudaError_t launch_element_fp64(const ElementArgs& a, const ElementLaunch& l, cudaStream_t stream);
+cudaError_t launch_element_fp32(const ElementArgs& a, const ElementLaunch& l, cudaStream_t stream);
+int         num_sms();
 
 // Node kernel: the end of step s (gather f_int, a = f/m, v += half*a, output
 // BCs) fused with the start of step s+1 (v += half*a, BCs, u += delta*v, BCs).
@@ -75,8 +94,10 @@ struct NodeArgs {
   const double*     inv_mass;
   const int*        bc_slot;  // [N] -1 or index into bcs
   const NodeBC*     bcs;
-  const StepSched*  sched;    // per-step schedule
+  const StepSched*  sched;    // per-step schedule [step][num_groups]
   const int*        step_base;// device step counter (schedule index of step "k = 0")
+  const int*        node_group; // [N] sample of each node, or null
+  int               num_groups;
   int               k_post;   // schedule offset of the step being finished, or -1
   int               k_pre;    // schedule offset of the step being started, or -1
   int               gather_only; // only f_int = gather(fe); no state update
@@ -99,8 +120,13 @@ cudaError_t launch_apply_bc(int N, long ld_n, const int* bc_slot, const NodeBC* 
 // two-pass deterministic sums into out[0], out[1].
 constexpr int kEnergyBlocks = 608;  // 4 x 152 SMs; partial buffer holds 2 doubles per block
 cudaError_t   launch_energies(int N, long ld_n, const double* mass, const double* v, int E, long ld_e,
-                              const int* conn, const double* u, const double* geo, double bulk, double shear,
-                              double* partial, double* out, cudaStream_t stream);
+                              const int* conn, const double* u, const double* geo, const int* elem_group,
+                              const GroupMaterial* mats, double* partial, double* out, cudaStream_t stream);
+
+// Per-sample max |field_c| over listed nodes (node ids global; sample from
+// node_group, or sample 0).  out: [num_groups], zeroed by the launcher.
+cudaError_t launch_group_max_abs(int count, const int* nodes, const double* field, long ld_n, int component,
+                                 const int* node_group, int num_groups, double* out, cudaStream_t stream);
 
 // Reference-layout views of SoA data ([E][8][9] / [E][8][6] / [N][3]).
 // which: 0 = F ([E][8][9]), 1 = sigma ([E][8][6]).

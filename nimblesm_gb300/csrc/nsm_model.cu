@@ -48,7 +48,8 @@ struct BcLine {
 }  // namespace
 
 struct nsm_model {
-  int          N = 0, E = 0;
+  int          N = 0, E = 0, S = 1;  // nodes, elements, samples
+  std::vector<int> node_off, elem_off;  // per-sample offsets [S+1]
   long         ld_n = 0, ld_e = 0;
   int          precision = NSM_PRECISION_FP64, store_ip = 1, graph_steps = 50, device = 0;
   double       density = 0, K = 0, G = 0, dt_crit = 0;
@@ -75,6 +76,13 @@ struct nsm_model {
   double* d_scratch = nullptr;  // energy partials / setup temporaries
   double* d_stage = nullptr;    // [3N] AoS staging for host copies
   double* d_out = nullptr;      // small results
+  double* d_group_out = nullptr;// [S] per-sample results
+  int*    d_elem_group = nullptr;  // [E] sample of each element (S > 1)
+  int*    d_node_group = nullptr;  // [N] sample of each node (S > 1)
+  int*    d_elem_off = nullptr;    // [S+1]
+  nsm::GroupMaterial* d_mats = nullptr;  // [S]
+  std::vector<double> dt_group;    // per-sample critical time step
+  nsm::ElementLaunch  elaunch{128, 0, 0};
 
   std::vector<BcLine> bcs;
   bool                bcs_dirty = true;
@@ -110,7 +118,8 @@ void free_all(nsm_model* m)
   void* ptrs[] = {m->d_conn, m->d_node_ptr, m->d_node_inc, m->d_X,     m->d_u,         m->d_v,     m->d_a,
                   m->d_f,    m->d_fext,     m->d_mass,     m->d_inv_mass, m->d_geo,    m->d_ip,    m->d_Xf,
                   m->d_uf,   m->d_fe,   m->d_status,   m->d_step_base, m->d_scratch, m->d_stage,  m->d_out,   m->d_bc_slot,
-                  m->d_bcs,  m->d_ibc_slot, m->d_ibcs,     m->d_sched};
+                  m->d_bcs,  m->d_ibc_slot, m->d_ibcs,     m->d_sched, m->d_group_out, m->d_elem_group,
+                  m->d_node_group, m->d_elem_off, m->d_mats};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (auto& e : m->ev_elem) {
@@ -173,6 +182,9 @@ int upload_bcs(nsm_model* m)
     NSM_CUDA(cudaStreamSynchronize(m->stream));  // host vectors go out of scope
   }
   m->bcs_dirty = false;
+  // captured graphs hold the old table's address
+  for (auto& g : m->graphs) cudaGraphExecDestroy(g.second);
+  m->graphs.clear();
   return NSM_OK;
 }
 
@@ -204,6 +216,10 @@ nsm::ElementArgs element_args(nsm_model* m, int k)
   a.shear     = m->G;
   a.ip        = m->d_ip;
   a.fe        = m->d_fe;
+  a.elem_group = m->d_elem_group;
+  a.mats       = m->d_mats;
+  a.num_groups = m->S;
+  a.persistent = 0;
   a.store_ip  = (k < 0 || m->store_ip) ? 1 : 0;
   a.sched     = k < 0 ? nullptr : m->d_sched;
   a.step_base = m->d_step_base;
@@ -227,6 +243,8 @@ nsm::NodeArgs node_args(nsm_model* m, int k_post, int k_pre, int gather_only)
   a.bcs         = m->d_bcs;
   a.sched       = m->d_sched;
   a.step_base   = m->d_step_base;
+  a.node_group  = m->d_node_group;
+  a.num_groups  = m->S;
   a.k_post      = k_post;
   a.k_pre       = k_pre;
   a.gather_only = gather_only;
@@ -249,8 +267,8 @@ cudaError_t sync_uf(nsm_model* m)
 cudaError_t launch_element(nsm_model* m, int k)
 {
   nsm::ElementArgs a = element_args(m, k);
-  return m->precision == NSM_PRECISION_FP64 ? nsm::launch_element_fp64(a, m->stream)
-                                            : nsm::launch_element_fp32(a, m->stream);
+  return m->precision == NSM_PRECISION_FP64 ? nsm::launch_element_fp64(a, m->elaunch, m->stream)
+                                            : nsm::launch_element_fp32(a, m->elaunch, m->stream);
 }
 
 std::pair<cudaEvent_t, cudaEvent_t> next_events(std::vector<std::pair<cudaEvent_t, cudaEvent_t>>& pool, size_t& used)
@@ -319,22 +337,42 @@ extern "C" {
 const char* nsm_last_error(void) { return g_error.c_str(); }
 int         nsm_abi_version(void) { return NSM_ABI_VERSION; }
 
-int nsm_create(const nsm_mesh_desc* mesh, const nsm_neohookean* material, const nsm_options* options,
-               nsm_model** out)
+}  // extern "C"
+
+namespace {
+
+// One handle over S samples: the samples' meshes are concatenated (node and
+// element ids offset per sample), each element carries its sample's material
+// and each node its sample's time schedule.  A single mesh is S = 1.
+int create_impl(int S, const nsm_mesh_desc* meshes, const nsm_neohookean* materials, const nsm_options* options,
+                nsm_model** out)
 {
-  if (!mesh || !material || !out) return fail(NSM_ERR_INVALID_ARGUMENT, "null argument");
+  if (!meshes || !materials || !out || S < 1) return fail(NSM_ERR_INVALID_ARGUMENT, "null argument");
   *out = nullptr;
-  if (mesh->num_nodes < 0 || mesh->num_elem < 0 || (mesh->num_elem > 0 && (!mesh->coords || !mesh->conn)))
-    return fail(NSM_ERR_INVALID_ARGUMENT, "invalid mesh");
-  if (!(material->density > 0) || !(material->bulk_modulus > 0) || !(material->shear_modulus >= 0))
-    return fail(NSM_ERR_INVALID_ARGUMENT, "invalid neo-Hookean parameters");
-  const int N = mesh->num_nodes, E = mesh->num_elem;
-  for (long i = 0; i < 8L * E; i++)
-    if (mesh->conn[i] < 0 || mesh->conn[i] >= N) return fail(NSM_ERR_INVALID_ARGUMENT, "connectivity out of range");
+  std::vector<int> node_off(S + 1, 0), elem_off(S + 1, 0);
+  for (int g = 0; g < S; g++) {
+    const nsm_mesh_desc& mesh = meshes[g];
+    if (mesh.num_nodes < 0 || mesh.num_elem < 0 || (mesh.num_elem > 0 && (!mesh.coords || !mesh.conn)))
+      return fail(NSM_ERR_INVALID_ARGUMENT, "invalid mesh");
+    const nsm_neohookean& mat = materials[g];
+    if (!(mat.density > 0) || !(mat.bulk_modulus > 0) || !(mat.shear_modulus >= 0))
+      return fail(NSM_ERR_INVALID_ARGUMENT, "invalid neo-Hookean parameters");
+    for (long i = 0; i < 8L * mesh.num_elem; i++)
+      if (mesh.conn[i] < 0 || mesh.conn[i] >= mesh.num_nodes)
+        return fail(NSM_ERR_INVALID_ARGUMENT, "connectivity out of range");
+    if ((long)node_off[g] + mesh.num_nodes > 2000000000L || (long)elem_off[g] + mesh.num_elem > 250000000L)
+      return fail(NSM_ERR_INVALID_ARGUMENT, "ensemble too large for 32-bit ids");
+    node_off[g + 1] = node_off[g] + mesh.num_nodes;
+    elem_off[g + 1] = elem_off[g] + mesh.num_elem;
+  }
+  const int N = node_off[S], E = elem_off[S];
 
   nsm_model* m = new nsm_model();
   m->N = N;
   m->E = E;
+  m->S = S;
+  m->node_off = node_off;
+  m->elem_off = elem_off;
   m->ld_n = pad(N > 0 ? N : 1, 64);
   m->ld_e = pad(E > 0 ? E : 1, 64);
   if (options) {
@@ -347,9 +385,13 @@ int nsm_create(const nsm_mesh_desc* mesh, const nsm_neohookean* material, const 
     delete m;
     return fail(NSM_ERR_INVALID_ARGUMENT, "unknown precision");
   }
-  m->density = material->density;
-  m->K       = material->bulk_modulus;
-  m->G       = material->shear_modulus;
+  m->density = materials[0].density;
+  m->K       = materials[0].bulk_modulus;
+  m->G       = materials[0].shear_modulus;
+  std::vector<nsm::GroupMaterial> gm(S);
+  for (int g = 0; g < S; g++)
+    gm[g] = nsm::GroupMaterial{materials[g].bulk_modulus, materials[g].shear_modulus, materials[g].density,
+                               std::sqrt(materials[g].bulk_modulus / materials[g].density)};
 
   auto bail = [&](int code) {
     free_all(m);
@@ -390,25 +432,49 @@ int nsm_create(const nsm_mesh_desc* mesh, const nsm_neohookean* material, const 
   NSM_CUDA_B(cudaMalloc(&m->d_step_base, sizeof(int)));
   NSM_CUDA_B(cudaMemsetAsync(m->d_step_base, 0, sizeof(int), m->stream));
   NSM_CUDA_B(cudaMalloc(&m->d_out, sizeof(double) * 8));
+  NSM_CUDA_B(cudaMalloc(&m->d_group_out, sizeof(double) * S));
   NSM_CUDA_B(cudaMalloc(&m->d_stage, nb));
+  NSM_CUDA_B(cudaMalloc(&m->d_mats, sizeof(nsm::GroupMaterial) * S));
+  NSM_CUDA_B(cudaMemcpyAsync(m->d_mats, gm.data(), sizeof(nsm::GroupMaterial) * S, cudaMemcpyHostToDevice, m->stream));
+  NSM_CUDA_B(cudaMalloc(&m->d_elem_off, sizeof(int) * (S + 1)));
+  NSM_CUDA_B(cudaMemcpyAsync(m->d_elem_off, elem_off.data(), sizeof(int) * (S + 1), cudaMemcpyHostToDevice, m->stream));
   size_t scratch = sizeof(double) * (E > 0 ? (size_t)E : 1);
   if (scratch < sizeof(double) * 2 * nsm::kEnergyBlocks) scratch = sizeof(double) * 2 * nsm::kEnergyBlocks;
   NSM_CUDA_B(cudaMalloc(&m->d_scratch, scratch + sizeof(double) * 1024));
 
   // host layouts -> device planes
   {
-    std::vector<int> conn_soa((size_t)8 * m->ld_e, 0);
-    for (long e = 0; e < E; e++)
-      for (int c = 0; c < 8; c++) conn_soa[(size_t)c * m->ld_e + e] = mesh->conn[8 * e + c];
+    std::vector<int>    conn_soa((size_t)8 * m->ld_e, 0);
     std::vector<double> X((size_t)3 * m->ld_n, 0.0);
-    for (long n = 0; n < N; n++)
-      for (int k = 0; k < 3; k++) X[(size_t)k * m->ld_n + n] = mesh->coords[3 * n + k];
+    std::vector<int>    egroup, ngroup;
+    if (S > 1) {
+      egroup.resize(E);
+      ngroup.resize(N);
+    }
+    std::vector<int> gconn((size_t)8 * E);
+    for (int g = 0; g < S; g++) {
+      const nsm_mesh_desc& mesh = meshes[g];
+      for (long e = 0; e < mesh.num_elem; e++) {
+        long ge = elem_off[g] + e;
+        for (int c = 0; c < 8; c++) {
+          int gid                          = node_off[g] + mesh.conn[8 * e + c];
+          conn_soa[(size_t)c * m->ld_e + ge] = gid;
+          gconn[8 * ge + c]                = gid;
+        }
+        if (S > 1) egroup[ge] = g;
+      }
+      for (long n = 0; n < mesh.num_nodes; n++) {
+        long gn = node_off[g] + n;
+        for (int k = 0; k < 3; k++) X[(size_t)k * m->ld_n + gn] = mesh.coords[3 * n + k];
+        if (S > 1) ngroup[gn] = g;
+      }
+    }
     // node -> (element, corner) incidence in increasing element order
     std::vector<int> ptr(N + 1, 0), inc((size_t)8 * E);
-    for (long i = 0; i < 8L * E; i++) ptr[mesh->conn[i] + 1]++;
+    for (long i = 0; i < 8L * E; i++) ptr[gconn[i] + 1]++;
     for (int n = 0; n < N; n++) ptr[n + 1] += ptr[n];
     std::vector<int> fill(ptr.begin(), ptr.end() - 1);
-    for (long i = 0; i < 8L * E; i++) inc[fill[mesh->conn[i]]++] = (int)i;
+    for (long i = 0; i < 8L * E; i++) inc[fill[gconn[i]]++] = (int)i;
     NSM_CUDA_B(cudaMemcpyAsync(m->d_conn, conn_soa.data(), sizeof(int) * conn_soa.size(), cudaMemcpyHostToDevice,
                                m->stream));
     NSM_CUDA_B(cudaMemcpyAsync(m->d_X, X.data(), sizeof(double) * X.size(), cudaMemcpyHostToDevice, m->stream));
@@ -418,37 +484,50 @@ int nsm_create(const nsm_mesh_desc* mesh, const nsm_neohookean* material, const 
     if (E > 0)
       NSM_CUDA_B(cudaMemcpyAsync(m->d_node_inc, inc.data(), sizeof(int) * inc.size(), cudaMemcpyHostToDevice,
                                  m->stream));
+    if (S > 1) {
+      NSM_CUDA_B(cudaMalloc(&m->d_elem_group, sizeof(int) * (E > 0 ? E : 1)));
+      NSM_CUDA_B(cudaMalloc(&m->d_node_group, sizeof(int) * (N > 0 ? N : 1)));
+      if (E > 0)
+        NSM_CUDA_B(cudaMemcpyAsync(m->d_elem_group, egroup.data(), sizeof(int) * E, cudaMemcpyHostToDevice, m->stream));
+      if (N > 0)
+        NSM_CUDA_B(cudaMemcpyAsync(m->d_node_group, ngroup.data(), sizeof(int) * N, cudaMemcpyHostToDevice, m->stream));
+    }
     NSM_CUDA_B(nsm::upload_shape_tables(m->stream));
 
-    // setup: geometry, lumped mass, critical time step
+    // setup: geometry, lumped mass, critical time step per sample
     double* me = nullptr;
     NSM_CUDA_B(cudaMalloc(&me, sizeof(double) * 8 * m->ld_e));
     nsm::SetupArgs s;
-    s.N = N;
-    s.E = E;
-    s.ld_n = m->ld_n;
-    s.ld_e = m->ld_e;
-    s.conn = m->d_conn;
-    s.X = m->d_X;
-    s.node_ptr = m->d_node_ptr;
-    s.node_inc = m->d_node_inc;
-    s.density = m->density;
-    s.sound_speed = std::sqrt(m->K / m->density);
-    s.geo = m->d_geo;
-    s.me = me;
-    s.dt_elem = m->d_scratch;
+    s.N          = N;
+    s.E          = E;
+    s.num_groups = S;
+    s.elem_group = m->d_elem_group;
+    s.elem_off   = m->d_elem_off;
+    s.mats       = m->d_mats;
+    s.ld_n       = m->ld_n;
+    s.ld_e       = m->ld_e;
+    s.conn       = m->d_conn;
+    s.X          = m->d_X;
+    s.node_ptr   = m->d_node_ptr;
+    s.node_inc   = m->d_node_inc;
+    s.geo        = m->d_geo;
+    s.me         = me;
+    s.dt_elem    = m->d_scratch;
     s.dt_partial = m->d_scratch + (scratch / sizeof(double));
-    s.dt_out = m->d_out;
-    s.mass = m->d_mass;
-    s.inv_mass = m->d_inv_mass;
-    s.status = m->d_status;
+    s.dt_out     = m->d_group_out;
+    s.mass       = m->d_mass;
+    s.inv_mass   = m->d_inv_mass;
+    s.status     = m->d_status;
     cudaError_t e = (E > 0) ? nsm::launch_setup(s, m->stream) : cudaSuccess;
-    double      dt = 1.7976931348623157e308;
-    if (e == cudaSuccess && E > 0) e = cudaMemcpyAsync(&dt, m->d_out, sizeof(double), cudaMemcpyDeviceToHost, m->stream);
+    m->dt_group.assign(S, 1.7976931348623157e308);
+    if (e == cudaSuccess && E > 0)
+      e = cudaMemcpyAsync(m->dt_group.data(), m->d_group_out, sizeof(double) * S, cudaMemcpyDeviceToHost, m->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(m->stream);  // host vectors live until here
     cudaFree(me);
     if (e != cudaSuccess) return bail(cuda_fail(e, "setup"));
-    m->dt_crit = dt;
+    m->dt_crit = 1.7976931348623157e308;
+    for (double d : m->dt_group)
+      if (d < m->dt_crit) m->dt_crit = d;
   }
   int st = read_status(m);
   if (st != NSM_OK) return bail(st);
@@ -456,6 +535,62 @@ int nsm_create(const nsm_mesh_desc* mesh, const nsm_neohookean* material, const 
   if (bc != NSM_OK) return bail(bc);
 #undef NSM_CUDA_B
   *out = m;
+  return NSM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int nsm_create(const nsm_mesh_desc* mesh, const nsm_neohookean* material, const nsm_options* options,
+               nsm_model** out)
+{
+  return create_impl(1, mesh, material, options, out);
+}
+
+int nsm_create_ensemble(int num_samples, const nsm_mesh_desc* meshes, const nsm_neohookean* materials,
+                        const nsm_options* options, nsm_model** out)
+{
+  return create_impl(num_samples, meshes, materials, options, out);
+}
+
+int nsm_ensemble_offsets(nsm_model* m, int* node_offsets, int* elem_offsets)
+{
+  if (!m) return fail(NSM_ERR_INVALID_ARGUMENT, "null model");
+  for (int g = 0; g <= m->S; g++) {
+    if (node_offsets) node_offsets[g] = m->node_off[g];
+    if (elem_offsets) elem_offsets[g] = m->elem_off[g];
+  }
+  return NSM_OK;
+}
+
+int nsm_ensemble_time_steps(nsm_model* m, double* dt)
+{
+  if (!m || !dt) return fail(NSM_ERR_INVALID_ARGUMENT, "null argument");
+  for (int g = 0; g < m->S; g++) dt[g] = m->dt_group[g];
+  return NSM_OK;
+}
+
+int nsm_ensemble_max_abs(nsm_model* m, int field, int component, const int* nodes, int count, double* out)
+{
+  if (!m || !out || (count > 0 && !nodes)) return fail(NSM_ERR_INVALID_ARGUMENT, "null argument");
+  double* src = field_ptr(m, field);
+  if (!src || component < 0 || component > 2) return fail(NSM_ERR_INVALID_ARGUMENT, "unknown field");
+  for (int i = 0; i < count; i++)
+    if (nodes[i] < 0 || nodes[i] >= m->N) return fail(NSM_ERR_INVALID_ARGUMENT, "node id out of range");
+  NSM_CUDA(cudaSetDevice(m->device));
+  int* d_nodes = nullptr;
+  if (count > 0) {
+    NSM_CUDA(cudaMalloc(&d_nodes, sizeof(int) * count));
+    NSM_CUDA(cudaMemcpyAsync(d_nodes, nodes, sizeof(int) * count, cudaMemcpyHostToDevice, m->stream));
+  }
+  cudaError_t e = nsm::launch_group_max_abs(count, d_nodes, src, m->ld_n, component, m->d_node_group, m->S,
+                                            m->d_group_out, m->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(out, m->d_group_out, sizeof(double) * m->S, cudaMemcpyDeviceToHost, m->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(m->stream);
+  if (d_nodes) cudaFree(d_nodes);
+  if (e != cudaSuccess) return cuda_fail(e, "nsm_ensemble_max_abs");
   return NSM_OK;
 }
 
@@ -479,8 +614,8 @@ int nsm_add_boundary_condition(nsm_model* m, int kind, int component, double val
   for (int n : b.nodes)
     if (n < 0 || n >= m->N) return fail(NSM_ERR_INVALID_ARGUMENT, "node set entry out of range");
   m->bcs.push_back(std::move(b));
-  m->bcs_dirty = true;
-  return upload_bcs(m);
+  m->bcs_dirty = true;  // uploaded when next needed
+  return NSM_OK;
 }
 
 int nsm_compute_lumped_mass(nsm_model* m, double* mass)
@@ -605,8 +740,8 @@ int nsm_get_energies(nsm_model* m, double* kinetic, double* internal)
 {
   if (!m) return fail(NSM_ERR_INVALID_ARGUMENT, "null model");
   NSM_CUDA(cudaSetDevice(m->device));
-  NSM_CUDA(nsm::launch_energies(m->N, m->ld_n, m->d_mass, m->d_v, m->E, m->ld_e, m->d_conn, m->d_u, m->d_geo, m->K,
-                                m->G, m->d_scratch, m->d_out + 2, m->stream));
+  NSM_CUDA(nsm::launch_energies(m->N, m->ld_n, m->d_mass, m->d_v, m->E, m->ld_e, m->d_conn, m->d_u, m->d_geo,
+                                m->d_elem_group, m->d_mats, m->d_scratch, m->d_out + 2, m->stream));
   double out[2];
   NSM_CUDA(cudaMemcpyAsync(out, m->d_out + 2, sizeof(out), cudaMemcpyDeviceToHost, m->stream));
   NSM_CUDA(cudaStreamSynchronize(m->stream));
@@ -615,26 +750,31 @@ int nsm_get_energies(nsm_model* m, double* kinetic, double* internal)
   return NSM_OK;
 }
 
-int nsm_begin(nsm_model* m, double initial_time, double final_time, int num_steps, int output_frequency,
-              const double* v_init)
+int nsm_begin_ensemble(nsm_model* m, double initial_time, const double* final_times, int num_steps,
+                       int output_frequency, const double* v_init)
 {
-  if (!m) return fail(NSM_ERR_INVALID_ARGUMENT, "null model");
+  if (!m || !final_times) return fail(NSM_ERR_INVALID_ARGUMENT, "null argument");
   if (num_steps < 0 || output_frequency < 0) return fail(NSM_ERR_INVALID_ARGUMENT, "negative step count");
-  if (final_time < initial_time) return fail(NSM_ERR_INVALID_ARGUMENT, "final time is less than initial time");
+  for (int g = 0; g < m->S; g++)
+    if (final_times[g] < initial_time) return fail(NSM_ERR_INVALID_ARGUMENT, "final time is less than initial time");
   NSM_CUDA(cudaSetDevice(m->device));
-  // schedule as src/integrators/explicit_time_integrator.cc:130-199 forms it
-  m->h_sched.assign(num_steps > 0 ? num_steps : 1, StepSched{0, 0, 0, 0});
-  m->h_time.assign(num_steps + 1, initial_time);
-  double t_cur = initial_time, t_prev = initial_time;
-  double dt_user = num_steps > 0 ? (final_time - initial_time) / num_steps : 0.0;
-  for (int s = 0; s < num_steps; s++) {
-    t_prev = t_cur;
-    t_cur += dt_user;
-    StepSched& q = m->h_sched[s];
-    q.delta      = t_cur - t_prev;
-    q.half       = 0.5 * q.delta;
-    q.is_output  = (output_frequency != 0 && (s % output_frequency == 0 || s == num_steps - 1)) ? 1 : 0;
-    m->h_time[s + 1] = t_cur;
+  // per-sample schedules as src/integrators/explicit_time_integrator.cc:130-199
+  // forms them, laid out [step][sample]
+  const int S = m->S;
+  m->h_sched.assign((size_t)(num_steps > 0 ? num_steps : 1) * S, StepSched{0, 0, 0, 0});
+  m->h_time.assign((size_t)(num_steps + 1), initial_time);
+  for (int g = 0; g < S; g++) {
+    double t_cur = initial_time, t_prev = initial_time;
+    double dt_user = num_steps > 0 ? (final_times[g] - initial_time) / num_steps : 0.0;
+    for (int s = 0; s < num_steps; s++) {
+      t_prev = t_cur;
+      t_cur += dt_user;
+      StepSched& q = m->h_sched[(size_t)s * S + g];
+      q.delta      = t_cur - t_prev;
+      q.half       = 0.5 * q.delta;
+      q.is_output  = (output_frequency != 0 && (s % output_frequency == 0 || s == num_steps - 1)) ? 1 : 0;
+      if (g == 0) m->h_time[s + 1] = t_cur;
+    }
   }
   if (m->d_sched) cudaFree(m->d_sched);
   m->d_sched = nullptr;
@@ -667,6 +807,14 @@ int nsm_begin(nsm_model* m, double initial_time, double final_time, int num_step
   return NSM_OK;
 }
 
+int nsm_begin(nsm_model* m, double initial_time, double final_time, int num_steps, int output_frequency,
+              const double* v_init)
+{
+  if (!m) return fail(NSM_ERR_INVALID_ARGUMENT, "null model");
+  std::vector<double> ft(m->S, final_time);
+  return nsm_begin_ensemble(m, initial_time, ft.data(), num_steps, output_frequency, v_init);
+}
+
 int nsm_advance(nsm_model* m, int num_steps)
 {
   if (!m) return fail(NSM_ERR_INVALID_ARGUMENT, "null model");
@@ -674,6 +822,8 @@ int nsm_advance(nsm_model* m, int num_steps)
   if (num_steps < 0 || m->steps_done + num_steps > m->num_steps)
     return fail(NSM_ERR_INVALID_ARGUMENT, "advance past the end of the schedule");
   NSM_CUDA(cudaSetDevice(m->device));
+  int r0 = upload_bcs(m);
+  if (r0) return r0;
   while (num_steps > 0) {
     int K = num_steps < m->graph_steps ? num_steps : m->graph_steps;
     if (m->profiling) {
@@ -756,6 +906,47 @@ int nsm_time_kernels(nsm_model* m, int repeats, double* element_ms, double* node
   cudaEventDestroy(c);
   if (element_ms) *element_ms = ms1 / repeats;
   if (node_ms) *node_ms = ms2 / repeats;
+  return read_status(m);
+}
+
+// Element-kernel launch shapes the autotuner tries: elements per block, and
+// one pass (one thread per element) or a persistent grid of blocks per SM
+// walking the elements of all samples.
+static const nsm::ElementLaunch kLaunchCandidates[] = {
+    {128, 0, 0}, {64, 0, 0}, {128, 1, 1}, {128, 1, 2}, {128, 1, 4}, {64, 1, 2}, {64, 1, 4}, {64, 1, 8},
+};
+static const int kNumLaunchCandidates = sizeof(kLaunchCandidates) / sizeof(kLaunchCandidates[0]);
+
+int nsm_autotune(nsm_model* m, int repeats, int* chosen, double* best_ms)
+{
+  if (!m || repeats <= 0) return fail(NSM_ERR_INVALID_ARGUMENT, "invalid argument");
+  NSM_CUDA(cudaSetDevice(m->device));
+  cudaEvent_t a, b;
+  NSM_CUDA(cudaEventCreate(&a));
+  NSM_CUDA(cudaEventCreate(&b));
+  int    best = 0;
+  double best_t = 1e300;
+  for (int c = 0; c < kNumLaunchCandidates; c++) {
+    m->elaunch = kLaunchCandidates[c];
+    NSM_CUDA(launch_element(m, -1));  // warm
+    cudaEventRecord(a, m->stream);
+    for (int r = 0; r < repeats; r++) NSM_CUDA(launch_element(m, -1));
+    cudaEventRecord(b, m->stream);
+    NSM_CUDA(cudaEventSynchronize(b));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, a, b);
+    if (ms < best_t) {
+      best_t = ms;
+      best   = c;
+    }
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  m->elaunch = kLaunchCandidates[best];
+  for (auto& g : m->graphs) cudaGraphExecDestroy(g.second);  // captured with the old shape
+  m->graphs.clear();
+  if (chosen) *chosen = best;
+  if (best_ms) *best_ms = best_t / repeats;
   return read_status(m);
 }
 

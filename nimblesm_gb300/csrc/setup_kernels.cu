@@ -70,11 +70,14 @@ __device__ __forceinline__ double invert3x3(const double m[3][3], double inv[3][
 // me[c][E]; and the element's stable time step L_e / sqrt(K/rho)
 // (src/nimble_block_base.cc:51-84, src/nimble_element.cc:221-260).
 __global__ void k_setup_elements(int E, long ld_e, const int* __restrict__ conn, const double* __restrict__ X,
-                                 long ld_n, double density, double sound_speed, double* __restrict__ geo,
-                                 double* __restrict__ me, double* __restrict__ dt_elem, int* __restrict__ status)
+                                 long ld_n, const int* __restrict__ elem_group, const GroupMaterial* __restrict__ mats,
+                                 double* __restrict__ geo, double* __restrict__ me, double* __restrict__ dt_elem,
+                                 int* __restrict__ status)
 {
   int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= E) return;
+  const GroupMaterial mat = mats[elem_group ? elem_group[e] : 0];
+  const double density = mat.density, sound_speed = mat.sound_speed;
   double x[8][3];
 #pragma unroll
   for (int n = 0; n < 8; n++) {
@@ -157,6 +160,22 @@ __global__ void k_gather_mass(int N, const int* __restrict__ node_ptr, const int
   inv_mass[n] = 1.0 / m;
 }
 
+// Minimum over each sample's contiguous element range: one block per sample.
+__global__ void k_group_min(const int* __restrict__ elem_off, const double* __restrict__ in, double* __restrict__ out)
+{
+  __shared__ double s[256];
+  const int         g = blockIdx.x;
+  double            v = 1.7976931348623157e308;
+  for (int i = elem_off[g] + threadIdx.x; i < elem_off[g + 1]; i += blockDim.x) v = fmin(v, in[i]);
+  s[threadIdx.x] = v;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) s[threadIdx.x] = fmin(s[threadIdx.x], s[threadIdx.x + w]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[g] = s[0];
+}
+
 // Deterministic minimum of n doubles: per-block minima, then one block.
 __global__ void k_min_reduce(long n, const double* __restrict__ in, double* __restrict__ out)
 {
@@ -175,14 +194,18 @@ __global__ void k_min_reduce(long n, const double* __restrict__ in, double* __re
 
 cudaError_t launch_setup(const SetupArgs& a, cudaStream_t stream)
 {
-  k_setup_elements<<<grid_for(a.E, 128), 128, 0, stream>>>(a.E, a.ld_e, a.conn, a.X, a.ld_n, a.density,
-                                                           a.sound_speed, a.geo, a.me, a.dt_elem, a.status);
+  k_setup_elements<<<grid_for(a.E, 128), 128, 0, stream>>>(a.E, a.ld_e, a.conn, a.X, a.ld_n, a.elem_group, a.mats,
+                                                           a.geo, a.me, a.dt_elem, a.status);
   k_gather_mass<<<grid_for(a.N, 256), 256, 0, stream>>>(a.N, a.node_ptr, a.node_inc, a.me, a.ld_e, a.mass,
                                                         a.inv_mass);
-  int blocks = grid_for(a.E, 256);
-  if (blocks > 1024) blocks = 1024;
-  k_min_reduce<<<blocks, 256, 0, stream>>>(a.E, a.dt_elem, a.dt_partial);
-  k_min_reduce<<<1, 256, 0, stream>>>(blocks, a.dt_partial, a.dt_out);
+  if (a.num_groups == 1) {
+    int blocks = grid_for(a.E, 256);
+    if (blocks > 1024) blocks = 1024;
+    k_min_reduce<<<blocks, 256, 0, stream>>>(a.E, a.dt_elem, a.dt_partial);
+    k_min_reduce<<<1, 256, 0, stream>>>(blocks, a.dt_partial, a.dt_out);
+  } else {
+    k_group_min<<<a.num_groups, 256, 0, stream>>>(a.elem_off, a.dt_elem, a.dt_out);
+  }
   return cudaGetLastError();
 }
 

@@ -79,6 +79,13 @@ SIGNATURES = {
     "nsm_launches_per_advance": (C.c_int, [_vp, C.c_int]),
     "nsm_set_profiling": (C.c_int, [_vp, C.c_int]),
     "nsm_get_profile": (C.c_int, [_vp, _dp, _ip, _dp, _ip]),
+    "nsm_create_ensemble": (C.c_int, [C.c_int, C.POINTER(_Mesh), C.POINTER(_Material), C.POINTER(_Options),
+                                      C.POINTER(_vp)]),
+    "nsm_ensemble_offsets": (C.c_int, [_vp, _ip, _ip]),
+    "nsm_ensemble_time_steps": (C.c_int, [_vp, _dp]),
+    "nsm_ensemble_max_abs": (C.c_int, [_vp, C.c_int, C.c_int, _ip, C.c_int, _dp]),
+    "nsm_begin_ensemble": (C.c_int, [_vp, C.c_double, _dp, C.c_int, C.c_int, _dp]),
+    "nsm_autotune": (C.c_int, [_vp, C.c_int, _ip, _dp]),
     "nsm_critical_time_step_noalloc": (C.c_int, [C.c_int, C.c_int, _vp, _vp, _vp, C.c_double, C.c_double, _vp,
                                                 _vp]),
     "nsm_host_alloc": (_vp, [C.c_size_t]),
@@ -131,27 +138,43 @@ class PinnedArray:
 
 
 class Model:
-    """Device-resident ModelData for one block of hex8 elements."""
+    """Device-resident ModelData for one block of hex8 elements (or, built
+    from several problems, an ensemble of independent samples in one handle)."""
 
-    def __init__(self, problem: Problem, precision: str = "fp64", store_ip_data: bool = True, device: int = 0,
+    def __init__(self, problem, precision: str = "fp64", store_ip_data: bool = True, device: int = 0,
                  graph_steps: int = 50):
         lib = library()
-        self.problem = problem
+        problems = list(problem) if isinstance(problem, (list, tuple)) else [problem]
+        self.problems = problems
+        self.problem = problems[0] if len(problems) == 1 else _concatenate(problems)
         self.precision = precision
-        coords = np.ascontiguousarray(problem.coords, dtype=np.float64)
-        conn = np.ascontiguousarray(problem.conn, dtype=np.int32)
-        mesh = _Mesh(problem.num_nodes, problem.num_elem, _d(coords), conn.ctypes.data_as(_ip))
-        mat = _Material(problem.density, problem.bulk_modulus, problem.shear_modulus)
+        keep = []
+        meshes = (_Mesh * len(problems))()
+        mats = (_Material * len(problems))()
+        for g, p in enumerate(problems):
+            coords = np.ascontiguousarray(p.coords, dtype=np.float64)
+            conn = np.ascontiguousarray(p.conn, dtype=np.int32)
+            keep += [coords, conn]
+            meshes[g] = _Mesh(p.num_nodes, p.num_elem, _d(coords), conn.ctypes.data_as(_ip))
+            mats[g] = _Material(p.density, p.bulk_modulus, p.shear_modulus)
         opt = _Options(PRECISION[precision], 1 if store_ip_data else 0, device, graph_steps)
         h = _vp()
-        _check(lib.nsm_create(C.byref(mesh), C.byref(mat), C.byref(opt), C.byref(h)))
+        if len(problems) == 1:
+            _check(lib.nsm_create(meshes, mats, C.byref(opt), C.byref(h)))
+        else:
+            _check(lib.nsm_create_ensemble(len(problems), meshes, mats, C.byref(opt), C.byref(h)))
         self._h = h
-        for bc in problem.bcs:
-            if bc.node_set not in problem.node_sets:
-                continue  # the reference drops lines naming an absent node set
-            nodes = np.ascontiguousarray(problem.node_sets[bc.node_set], dtype=np.int32)
-            _check(lib.nsm_add_boundary_condition(h, bc.kind, bc.component, bc.value,
-                                                  nodes.ctypes.data_as(_ip), len(nodes)))
+        S = len(problems)
+        no, eo = np.zeros(S + 1, np.int32), np.zeros(S + 1, np.int32)
+        _check(lib.nsm_ensemble_offsets(h, no.ctypes.data_as(_ip), eo.ctypes.data_as(_ip)))
+        self.node_offsets, self.elem_offsets = no, eo
+        for g, p in enumerate(problems):
+            for bc in p.bcs:
+                if bc.node_set not in p.node_sets:
+                    continue  # the reference drops lines naming an absent node set
+                nodes = np.ascontiguousarray(np.asarray(p.node_sets[bc.node_set]) + no[g], dtype=np.int32)
+                _check(lib.nsm_add_boundary_condition(h, bc.kind, bc.component, bc.value,
+                                                      nodes.ctypes.data_as(_ip), len(nodes)))
 
     def close(self):
         if getattr(self, "_h", None):
@@ -210,11 +233,37 @@ class Model:
 
     # ---- explicit loop ----
     def begin(self, final_time, num_steps, output_frequency=0, initial_time=0.0, v_init="problem"):
+        """final_time: a number, or one per sample for an ensemble."""
         if isinstance(v_init, str):
             v_init = self.problem.v_init
         v = None if v_init is None else np.ascontiguousarray(v_init, dtype=np.float64)
-        _check(library().nsm_begin(self._h, initial_time, final_time, num_steps, output_frequency,
-                                   None if v is None else _d(v)))
+        ft = np.ascontiguousarray(np.broadcast_to(np.asarray(final_time, np.float64), (len(self.problems),)))
+        _check(library().nsm_begin_ensemble(self._h, initial_time, _d(ft), num_steps, output_frequency,
+                                            None if v is None else _d(v)))
+
+    # ---- ensemble ----
+    def sample_time_steps(self):
+        dt = np.zeros(len(self.problems))
+        _check(library().nsm_ensemble_time_steps(self._h, _d(dt)))
+        return dt
+
+    def sample_max_abs(self, label, component, node_sets):
+        """Per-sample max |field component| over node_sets[g] (local ids of
+        sample g)."""
+        ids = np.ascontiguousarray(np.concatenate([np.asarray(ns, np.int64) + self.node_offsets[g]
+                                                   for g, ns in enumerate(node_sets)]), dtype=np.int32)
+        out = np.zeros(len(self.problems))
+        _check(library().nsm_ensemble_max_abs(self._h, FIELDS[label], component, ids.ctypes.data_as(_ip),
+                                              len(ids), _d(out)))
+        return out
+
+    def sample_slice(self, g):
+        return slice(int(self.node_offsets[g]), int(self.node_offsets[g + 1]))
+
+    def autotune(self, repeats=5):
+        c, ms = C.c_int(), C.c_double()
+        _check(library().nsm_autotune(self._h, repeats, C.byref(c), C.byref(ms)))
+        return c.value, ms.value
 
     def advance(self, num_steps):
         _check(library().nsm_advance(self._h, int(num_steps)))
@@ -264,6 +313,19 @@ class Model:
         _check(library().nsm_get_profile(self._h, C.byref(te), C.byref(ne), C.byref(tn), C.byref(nn)))
         return {"element_ms": te.value, "element_launches": ne.value, "node_ms": tn.value,
                 "node_launches": nn.value}
+
+
+def _concatenate(problems):
+    """The ensemble's problems as one mesh with offset ids (host view)."""
+    no = np.cumsum([0] + [p.num_nodes for p in problems])
+    coords = np.concatenate([p.coords for p in problems])
+    conn = np.concatenate([p.conn + no[g] for g, p in enumerate(problems)]).astype(np.int32)
+    v0 = None
+    if all(p.v_init is not None for p in problems):
+        v0 = np.concatenate([p.v_init for p in problems])
+    return Problem(coords=coords, conn=conn, node_sets={}, density=problems[0].density,
+                   bulk_modulus=problems[0].bulk_modulus, shear_modulus=problems[0].shear_modulus, bcs=[],
+                   v_init=v0)
 
 
 def run(problem: Problem, final_time: float, num_steps: int, output_frequency: int = 0,

@@ -172,3 +172,20 @@ def critical_time_step(problem: Problem) -> float:
     min over elements of L_e / sqrt(K / rho)."""
     c = np.sqrt(problem.bulk_modulus / problem.density)
     return float((characteristic_lengths(problem.coords, problem.conn) / c).min())
+
+
+def uq_ensemble(num_samples: int = 512, n_min: int = 8, n_max: int = 48, seed: int = 0, jitter: float = 0.2,
+                cov: float = 0.10, bulk_mean: float = 160e9, shear_mean: float = 79.3e9,
+                density: float = 7800.0) -> list:
+    """Uncertainty-quantification ensemble: sample g is a jittered cube with
+    n_g^3 hexes, n_g ~ U{n_min..n_max}, and log-normal bulk and shear moduli
+    (given means, coefficient of variation cov), the unit-cube boundary
+    conditions and initial velocity of cube_problem.  All draws are seeded."""
+    rng = np.random.default_rng(seed)
+    sig = np.sqrt(np.log1p(cov * cov))
+    ns = rng.integers(n_min, n_max + 1, size=num_samples)
+    K = np.exp(np.log(bulk_mean) - 0.5 * sig * sig + sig * rng.standard_normal(num_samples))
+    G = np.exp(np.log(shear_mean) - 0.5 * sig * sig + sig * rng.standard_normal(num_samples))
+    return [cube_problem(int(ns[g]), jitter=jitter, seed=seed * 100003 + g, density=density,
+                         bulk_modulus=float(K[g]), shear_modulus=float(G[g])) for g in range(num_samples)]
+

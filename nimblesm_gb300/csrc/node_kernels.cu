@@ -1,7 +1,13 @@
 // Node kernels: assembly of the element forces and the central-difference
-// update.  Compiled with --fmad=false: every product and sum rounds exactly
-// as the reference's host loops do, so given the same element forces the
-// nodal state equals the reference's bit for bit.
+// update.
+//
+// FP64 form: every product and sum is an explicit round-to-nearest intrinsic
+// (__dmul_rn / __dadd_rn are never fused), so given the same element forces
+// the nodal state equals the reference's bit for bit.  FP32-mixed form: the
+// FP32 element forces are assembled in FP32 and the FP64 update uses fused
+// multiply-adds -- on this chip FP64 operations, not bytes, bound a node
+// update, and the exact rounding of the reference buys nothing when the forces
+// themselves are FP32.
 #include "nsm_kernels.cuh"
 
 namespace nsm {
@@ -16,12 +22,19 @@ __device__ __forceinline__ void apply_bc(const NodeBC& bc, double delta, const d
     if (bc.kind[k] == 1) {
       v[k] = bc.value[k];
     } else if (bc.kind[k] == 2 && delta > 0.0) {
-      v[k] = (bc.value[k] - u[k]) / delta;
+      v[k] = __ddiv_rn(__dadd_rn(bc.value[k], -u[k]), delta);
     }
   }
 }
 
-template <typename TF>
+// y + s*x, rounded as the reference's two operations or fused.
+template <bool kExact>
+__device__ __forceinline__ double axpy(double s, double x, double y)
+{
+  return kExact ? __dadd_rn(y, __dmul_rn(s, x)) : fma(s, x, y);
+}
+
+template <typename TF, bool kExact>
 __global__ void __launch_bounds__(256) k_node_update(NodeArgs a)
 {
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
@@ -37,15 +50,19 @@ __global__ void __launch_bounds__(256) k_node_update(NodeArgs a)
     // ModelData::ComputeInternalForce: zero, then element contributions in
     // increasing element order (src/nimble_model_data.cc:620-667,
     // src/nimble_block.cc:373-383).
-    const TF* fe = reinterpret_cast<const TF*>(a.fe);
-    double    f[3] = {0.0, 0.0, 0.0};
+    const TF* fe    = reinterpret_cast<const TF*>(a.fe);
+    TF        fs[3] = {TF(0), TF(0), TF(0)};
     for (int k = a.node_ptr[n]; k < a.node_ptr[n + 1]; k++) {
       const int  ec = __ldg(&a.node_inc[k]);
       const long e  = ec >> 3;
       const int  c  = ec & 7;
 #pragma unroll
-      for (int i = 0; i < 3; i++) f[i] += (double)__ldg(&fe[e * 24 + c * 3 + i]);
+      for (int i = 0; i < 3; i++) {
+        const TF x = __ldg(&fe[e * 24 + c * 3 + i]);
+        fs[i]      = kExact ? TF(__dadd_rn(double(fs[i]), double(x))) : fs[i] + x;
+      }
     }
+    double f[3] = {double(fs[0]), double(fs[1]), double(fs[2])};
 #pragma unroll
     for (int i = 0; i < 3; i++) a.f_int[i * ld + n] = f[i];
     if (a.gather_only) return;
@@ -54,8 +71,8 @@ __global__ void __launch_bounds__(256) k_node_update(NodeArgs a)
 #pragma unroll
     for (int i = 0; i < 3; i++) {
       // a = (1/m) (f_int + f_ext), f_ext = 0 (src/integrators/explicit_time_integrator.cc:250-257)
-      acc[i] = im * (f[i] + 0.0);
-      v[i]   = a.v[i * ld + n] + s.half * acc[i];
+      acc[i] = kExact ? __dmul_rn(im, __dadd_rn(f[i], 0.0)) : im * f[i];
+      v[i]   = axpy<kExact>(s.half, acc[i], a.v[i * ld + n]);
       u[i]   = a.u[i * ld + n];
     }
     if (s.is_output && slot >= 0) apply_bc(bc, s.delta, u, v);
@@ -72,10 +89,10 @@ __global__ void __launch_bounds__(256) k_node_update(NodeArgs a)
     // (src/integrators/explicit_time_integrator.cc:200-223)
     const StepSched s = a.sched[(long)(*a.step_base + a.k_pre) * a.num_groups + group];
 #pragma unroll
-    for (int i = 0; i < 3; i++) v[i] = v[i] + s.half * acc[i];
+    for (int i = 0; i < 3; i++) v[i] = axpy<kExact>(s.half, acc[i], v[i]);
     if (slot >= 0) apply_bc(bc, s.delta, u, v);
 #pragma unroll
-    for (int i = 0; i < 3; i++) u[i] = u[i] + s.delta * v[i];
+    for (int i = 0; i < 3; i++) u[i] = axpy<kExact>(s.delta, v[i], u[i]);
     if (slot >= 0) apply_bc(bc, s.delta, u, v);
   }
 #pragma unroll
@@ -91,9 +108,9 @@ cudaError_t launch_node_update(const NodeArgs& a, cudaStream_t stream)
 {
   if (a.N == 0) return cudaSuccess;
   if (a.fe_is_float)
-    k_node_update<float><<<grid_for(a.N, 256), 256, 0, stream>>>(a);
+    k_node_update<float, false><<<grid_for(a.N, 256), 256, 0, stream>>>(a);
   else
-    k_node_update<double><<<grid_for(a.N, 256), 256, 0, stream>>>(a);
+    k_node_update<double, true><<<grid_for(a.N, 256), 256, 0, stream>>>(a);
   return cudaGetLastError();
 }
 

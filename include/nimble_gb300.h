@@ -224,6 +224,12 @@ int nsm_critical_time_step_noalloc(int num_nodes, int num_elem, const double* co
                                    const int* conn, double density, double bulk_modulus, double* dt_out,
                                    void* stream);
 
+/* Diagnostic: D[128][N] = A[128][K] * B[N][K]^T on the 5th-generation
+ * tensor cores (operands rounded to BF16, FP32 accumulation), through the
+ * same primitives and shared-memory layout as the learned closure's kernels.
+ * N, K multiples of 16, N <= 256, K <= 128; host arrays. */
+int nsm_tc_selftest(int N, int K, const float* A, const float* B, float* D);
+
 /* Pinned host memory for the host-buffer entry points (page-locked so that the
  * copies run at full link bandwidth). */
 void* nsm_host_alloc(size_t bytes);

@@ -49,6 +49,7 @@ class _Options(C.Structure):
 
 
 _dp = C.POINTER(C.c_double)
+_dp_f = C.POINTER(C.c_float)
 _ip = C.POINTER(C.c_int)
 _vp = C.c_void_p
 
@@ -88,6 +89,7 @@ SIGNATURES = {
     "nsm_autotune": (C.c_int, [_vp, C.c_int, _ip, _dp]),
     "nsm_critical_time_step_noalloc": (C.c_int, [C.c_int, C.c_int, _vp, _vp, _vp, C.c_double, C.c_double, _vp,
                                                 _vp]),
+    "nsm_tc_selftest": (C.c_int, [C.c_int, C.c_int, _dp_f, _dp_f, _dp_f]),
     "nsm_host_alloc": (_vp, [C.c_size_t]),
     "nsm_host_free": (None, [_vp]),
 }

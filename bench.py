@@ -204,6 +204,81 @@ def uq_variants(E, args, device):
     return out
 
 
+def big_fp32_variant(E, args, device):
+    """The FP32-mixed form on a 256^3 jittered cube (16.8M elements), with its
+    displacement error against the FP64 form on the same mesh and steps."""
+    n = args.big_n
+    prob = cube_problem(n, jitter=0.2, seed=0)
+    dt = 0.5 * critical_time_step(prob)
+    steps = args.big_steps
+    out = {}
+    u = {}
+    for precision in ("fp32", "fp64"):
+        m = E.Model(prob, precision=precision, device=device)
+        m.begin(SCHEDULE_STEPS * dt, SCHEDULE_STEPS, SCHEDULE_STEPS)
+        m.advance(3)
+        m.synchronize()
+        ms = m.advance_timed(steps)
+        u[precision] = m.GetVectorNodeData("displacement")
+        out[precision] = 8.0 * prob.num_elem * steps / (ms * 1e-3)
+        m.close()
+    err = float(np.linalg.norm(u["fp32"] - u["fp64"]) / np.linalg.norm(u["fp64"]))
+    return {f"fp32_{n}cube": {"value": out["fp32"], "unit": UNIT, "elements": prob.num_elem, "steps_timed": steps,
+                              "fp64_value": out["fp64"], "speedup_vs_fp64": out["fp32"] / out["fp64"],
+                              "rel_disp_err_vs_fp64": err, "after_steps": 3 + steps}}
+
+
+def mlp_variant(E, args, problem, device, fp64_value, fp32_value):
+    """The learned closure: generated and trained on the GPU (tensor-core
+    forward/backward), then fused into the element kernel of the 128^3 run.
+    Errors against the FP64 plain form at the same step; speedups against the
+    FP64 and FP32 plain forms."""
+    t0 = time.perf_counter()
+    mlp = E.MLPClosure(problem.bulk_modulus, problem.shear_modulus, seed=1, device=device)
+    mlp.generate(args.mlp_pairs, seed=7, perturbation=0.05, min_det=0.5)
+    t1 = time.perf_counter()
+    loss = mlp.train(epochs=args.mlp_epochs, batch_tiles=16, lr=5e-3)
+    t2 = time.perf_counter()
+    dt = 0.5 * critical_time_step(problem)
+    steps = args.mlp_steps
+    res = {}
+    for form in ("mlp", "fp64"):
+        m = E.Model(problem, precision="fp32" if form == "mlp" else "fp64", device=device)
+        if form == "mlp":
+            m.set_closure(mlp)
+        m.begin(SCHEDULE_STEPS * dt, SCHEDULE_STEPS, SCHEDULE_STEPS)
+        m.advance(1)
+        e0 = sum(m.GetEnergies())
+        m.synchronize()
+        if form == "mlp":
+            m.set_profiling(True)
+            m.advance(2)
+            prof = m.get_profile()
+            m.set_profiling(False)
+            ms = m.advance_timed(steps - 3)
+        else:
+            m.advance(steps - 1)
+            ms = None
+        ke, ie = m.GetEnergies()
+        F, sig = m.GetIntegrationPointData()
+        res[form] = dict(u=m.GetVectorNodeData("displacement"), sig=sig, drift=(ke + ie - e0) / e0, ms=ms,
+                         fallbacks=m.closure_fallbacks(), prof=prof if form == "mlp" else None)
+        m.close()
+    mlp.close()
+    a, b = res["mlp"], res["fp64"]
+    value = 8.0 * problem.num_elem * (steps - 3) / (a["ms"] * 1e-3)
+    return {"mlp_closure": {
+        "value": value, "unit": UNIT, "ms_per_step": a["ms"] / (steps - 3),
+        "element_launch_ms": a["prof"]["element_ms"] / max(a["prof"]["element_launches"], 1),
+        "speedup_vs_fp64": value / fp64_value, "speedup_vs_fp32": value / fp32_value,
+        "rel_disp_err_vs_fp64": float(np.linalg.norm(a["u"] - b["u"]) / np.linalg.norm(b["u"])),
+        "rel_stress_err_vs_fp64": float(np.linalg.norm(a["sig"] - b["sig"]) / np.linalg.norm(b["sig"])),
+        "energy_drift": a["drift"], "energy_drift_fp64": b["drift"], "after_steps": steps,
+        "envelope_fallbacks": a["fallbacks"], "training_pairs": args.mlp_pairs, "epochs": args.mlp_epochs,
+        "final_loss": loss, "generate_s": t1 - t0, "train_s": t2 - t1,
+        "network": "9-64-64-6 GELU, BF16 weights/activations, FP32 accumulate, tcgen05; linear skip, quadratic gate"}}
+
+
 def run_ours(args):
     from nimblesm_gb300 import engine as E
 
@@ -318,6 +393,11 @@ def run_ours(args):
                           "clocks": r["clocks"]}
     if args.uq_steps > 0:
         variants.update(uq_variants(E, args, local if ws > 1 else 0))
+    if args.big_steps > 0:
+        variants.update(big_fp32_variant(E, args, local if ws > 1 else 0))
+    if args.mlp_steps > 0:
+        fp32_value = variants.get("fp32", {}).get("value", float("nan"))
+        variants.update(mlp_variant(E, args, problem, local if ws > 1 else 0, value / ws, fp32_value / ws))
     if variants:
         line["variants"] = variants
     if rank == 0 and not args.no_cpu_baseline:
@@ -342,6 +422,11 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--uq-steps", type=int, default=100, help="timed steps of the 512-sample ensemble (0: skip)")
     ap.add_argument("--uq-samples", type=int, default=512)
+    ap.add_argument("--big-n", type=int, default=256, help="cube divisions of the large FP32-mixed variant")
+    ap.add_argument("--big-steps", type=int, default=20, help="timed steps of the large variant (0: skip)")
+    ap.add_argument("--mlp-steps", type=int, default=103, help="steps of the learned-closure run (0: skip)")
+    ap.add_argument("--mlp-pairs", type=int, default=4_000_000)
+    ap.add_argument("--mlp-epochs", type=int, default=20)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -224,6 +224,53 @@ int nsm_critical_time_step_noalloc(int num_nodes, int num_elem, const double* co
                                    const int* conn, double density, double bulk_modulus, double* dt_out,
                                    void* stream);
 
+/* ---- Learned constitutive closure ----
+ * A 9 -> 64 -> 64 -> 6 MLP (GELU, BF16 weights, FP32 accumulation, trained
+ * and evaluated on the 5th-generation tensor cores) that maps H = F - I to
+ * the Cauchy stress over the shear modulus, standing in for the neo-Hookean
+ * material update behind the same material interface (the reference's
+ * Material::GetStress, src/nimble_material.h:239-313; no learned material
+ * exists in the reference).  It is placed on the material's small-strain
+ * linear map with a quadratic gate: sigma/G = L(H) + s_r |x|^2 MLP(x),
+ * x = H * in_scale, so it reduces to the exact small-strain response near
+ * F = I.  Points outside the
+ * training envelope (|H_ij| > 4 s_in^-1 or det F < min_det) use the plain
+ * neo-Hookean stress.  Parameters: W1[64][9], b1[64], W2[64][64], b2[64],
+ * W3[6][64], b3[6] (NSM_MLP_PARAMS floats); scales: in_scale, res_scale,
+ * K/G, envelope, min_det. */
+#define NSM_MLP_PARAMS 5190
+typedef struct nsm_mlp nsm_mlp;
+const char* nsm_mlp_last_error(void);
+int nsm_mlp_create(double bulk_modulus, double shear_modulus, unsigned long long seed, int device, nsm_mlp** out);
+int nsm_mlp_destroy(nsm_mlp* mlp);
+/* Training set on the device: n pairs F = I + N(0, perturbation^2) per entry,
+ * det F >= min_det (rejection), sigma from the neo-Hookean material. */
+int nsm_mlp_generate(nsm_mlp* mlp, long n, unsigned long long seed, double perturbation, double min_det);
+/* Adam on the mean squared error of the scaled residual, minibatches of
+ * 128 * batch_tiles points, cosine learning-rate decay; returns the last
+ * epoch's mean loss per output component. */
+int nsm_mlp_train(nsm_mlp* mlp, int epochs, int batch_tiles, double lr, double* final_loss);
+int nsm_mlp_get_params(nsm_mlp* mlp, float* params, float* scales);
+/* Copy of training pairs [first, first + count): H [count][9], sigma/G [count][6]. */
+int nsm_mlp_training_sample(nsm_mlp* mlp, long first, long count, float* H, float* Y);
+int nsm_mlp_set_params(nsm_mlp* mlp, const float* params, const float* scales);
+/* Gradient of the training loss over n given pairs (H row-major [n][9],
+ * sigma/G [n][6]) with respect to the parameters, as the training kernel
+ * computes it; loss = mean over points of the squared scaled residual. */
+int nsm_mlp_gradient(nsm_mlp* mlp, long n, const float* H, const float* Y, float* grad, double* loss);
+/* Stress of n deformation gradients (reference slot order [n][9]) -> sigma
+ * [n][6]; fallback_count = points outside the envelope (plain material). */
+int nsm_mlp_predict(nsm_mlp* mlp, long n, const double* F, double* sigma, int* fallback_count);
+
+/* Use the learned closure as the material of a model's element kernel (the
+ * FP32-mixed form, one material; NULL restores the neo-Hookean stress).  The
+ * closure's parameters are read at every launch, so training may continue
+ * between steps.  nsm_closure_fallbacks: integration-point evaluations that
+ * left the training envelope and used the plain material, since the model
+ * was created. */
+int nsm_set_mlp_closure(nsm_model* model, nsm_mlp* closure);
+int nsm_closure_fallbacks(nsm_model* model, unsigned long long* count);
+
 /* Diagnostic: D[128][N] = A[128][K] * B[N][K]^T on the 5th-generation
  * tensor cores (operands rounded to BF16, FP32 accumulation), through the
  * same primitives and shared-memory layout as the learned closure's kernels.

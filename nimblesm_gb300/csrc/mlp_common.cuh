@@ -1,0 +1,127 @@
+// The learned constitutive closure: a 9 -> 64 -> 64 -> 6 MLP (GELU) mapping
+// the displacement gradient H = F - I to the Cauchy stress over the shear
+// modulus, with BF16 weights and FP32 accumulation on the 5th-generation
+// tensor cores.
+//
+// The network is placed on a linear skip and a quadratic gate:
+//   sigma / G = L(H) + s_r * |x|^2 * MLP(x),   x = H * in_scale,
+// where L is the small-strain limit of the neo-Hookean stress
+// (K/G tr(eps) I + 2 dev(eps), eps = sym H).  The remainder sigma/G - L(H) is
+// O(|H|^2), so the network learns the bounded, direction-dependent ratio
+// (sigma/G - L) / |x|^2, and its own error is multiplied by |x|^2: at the
+// strains of a dynamic run (~1e-3) the closure reduces to the exact
+// small-strain response instead of carrying a BF16 network's absolute error
+// floor as a spurious stress.
+//
+// Parameters (FP32 master copy, kParams floats): W1[64][9], b1[64], W2[64][64],
+// b2[64], W3[6][64], b3[6].  BF16 operand images in the shared-memory tile
+// layout of tc05.cuh are derived from them after every update:
+//   W1x [64][32]: columns 0-8 W1, 9 b1, 16-24 W1 again.  The input row is
+//                 [hi(x) (9), 1, 0 x6, lo(x) (9), 0 x7] with hi = bf16(x) and
+//                 lo = bf16(x - hi): a two-term BF16 split of the input, so the
+//                 first layer sees the input to ~16 significant bits, and the
+//                 bias rides in the constant column.
+//   W2  [64][64], W3x [16][64] (rows 0-5 W3), and for the backward pass the
+//   transposes W2t [64][64] and W3t [64][16].
+#pragma once
+
+#include <cuda_bf16.h>
+
+#include "tc05.cuh"
+
+namespace nsm {
+namespace mlp {
+
+constexpr int kIn = 9, kHid = 64, kOut = 6;
+constexpr int kInX  = 32;  // extended input width (two-term split + bias column)
+constexpr int kOutX = 16;  // padded output width
+constexpr int oW1 = 0, ob1 = oW1 + kHid * kIn, oW2 = ob1 + kHid, ob2 = oW2 + kHid * kHid, oW3 = ob2 + kHid,
+              ob3 = oW3 + kOut * kHid, kParams = ob3 + kOut;  // 5190
+
+// operand images (bytes), in the order they are laid out
+constexpr int kImgW1 = kHid * kInX * 2, kImgW2 = kHid * kHid * 2, kImgW3 = kOutX * kHid * 2,
+              kImgW2t = kHid * kHid * 2, kImgW3t = kHid * kOutX * 2;
+constexpr int kOffW1 = 0, kOffW2 = kOffW1 + kImgW1, kOffW3 = kOffW2 + kImgW2, kOffW2t = kOffW3 + kImgW3,
+              kOffW3t = kOffW2t + kImgW2t, kImgBytes = kOffW3t + kImgW3t;  // 24576
+
+struct Scales {
+  float in_scale;   // x = H * in_scale (1 / perturbation)
+  float res_scale;  // s_r: rms of (sigma/G - L(H)) / |x|^2 over the training set
+  float k_over_g;   // bulk / shear of the trained material
+  float envelope;   // |H_ij| bound of the training envelope
+  float min_det;    // det F bound of the training envelope
+};
+
+__device__ __forceinline__ float gelu(float z) { return 0.5f * z * (1.0f + erff(z * 0.70710678118654752f)); }
+__device__ __forceinline__ float gelu_grad(float z)
+{
+  return 0.5f * (1.0f + erff(z * 0.70710678118654752f)) + z * 0.39894228040143268f * __expf(-0.5f * z * z);
+}
+
+// Small-strain limit of the neo-Hookean stress over G, symmetric order.
+__device__ __forceinline__ void linear_part(const float x[9], float k_over_g, float L[6])
+{
+  const float tr = x[0] + x[4] + x[8];
+  const float a  = k_over_g * tr, d = tr * (1.0f / 3.0f);
+  L[0]           = a + 2.0f * (x[0] - d);
+  L[1]           = a + 2.0f * (x[4] - d);
+  L[2]           = a + 2.0f * (x[8] - d);
+  L[3]           = x[1] + x[3];
+  L[4]           = x[5] + x[7];
+  L[5]           = x[6] + x[2];
+}
+
+// The quadratic gate |x|^2 (floored so the training target stays finite).
+__device__ __forceinline__ float gate(const float xs[9])
+{
+  float g = 0.0f;
+#pragma unroll
+  for (int j = 0; j < 9; j++) g += xs[j] * xs[j];
+  return fmaxf(g, 1e-12f);
+}
+
+// Inside the training envelope: every |H_ij| <= envelope and det F >= min_det.
+__device__ __forceinline__ bool in_envelope(const float h[9], const Scales& s)
+{
+  float m = 0.0f;
+#pragma unroll
+  for (int j = 0; j < 9; j++) m = fmaxf(m, fabsf(h[j]));
+  const float f00 = 1 + h[0], f11 = 1 + h[4], f22 = 1 + h[8];
+  const float det = f00 * (f11 * f22 - h[5] * h[7]) - h[1] * (h[3] * f22 - h[5] * h[6]) + h[2] * (h[3] * h[7] - f11 * h[6]);
+  return m <= s.envelope && det >= s.min_det;
+}
+
+// Write 8 consecutive features (one 16-byte chunk) of row r of a K-major tile.
+__device__ __forceinline__ void store_chunk(uint8_t* tile, int r, int k0, int K, const float* v)
+{
+  __nv_bfloat162 p0 = __floats2bfloat162_rn(v[0], v[1]), p1 = __floats2bfloat162_rn(v[2], v[3]),
+                 p2 = __floats2bfloat162_rn(v[4], v[5]), p3 = __floats2bfloat162_rn(v[6], v[7]);
+  uint4 w;
+  w.x = *reinterpret_cast<uint32_t*>(&p0);
+  w.y = *reinterpret_cast<uint32_t*>(&p1);
+  w.z = *reinterpret_cast<uint32_t*>(&p2);
+  w.w = *reinterpret_cast<uint32_t*>(&p3);
+  *reinterpret_cast<uint4*>(tile + tc::kmajor_offset(r, k0, K)) = w;
+}
+
+__device__ __forceinline__ void store_bf16(uint8_t* tile, int r, int k, int K, float v)
+{
+  *reinterpret_cast<__nv_bfloat16*>(tile + tc::kmajor_offset(r, k, K)) = __float2bfloat16_rn(v);
+}
+
+// The extended input row [hi(x), 1, 0.., lo(x), 0..] of one point.
+__device__ __forceinline__ void input_row(const float x[9], float row[kInX])
+{
+#pragma unroll
+  for (int j = 0; j < kInX; j++) row[j] = 0.0f;
+#pragma unroll
+  for (int j = 0; j < 9; j++) {
+    const float hi = __bfloat162float(__float2bfloat16_rn(x[j]));
+    row[j]         = hi;
+    row[16 + j]    = x[j] - hi;
+  }
+  row[9] = 1.0f;
+}
+
+}  // namespace mlp
+}  // namespace nsm

@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "../../include/nimble_gb300.h"
+#include "mlp_element.cuh"
 #include "nsm_kernels.cuh"
 
 using nsm::NodeBC;
@@ -83,6 +84,8 @@ struct nsm_model {
   nsm::GroupMaterial* d_mats = nullptr;  // [S]
   std::vector<double> dt_group;    // per-sample critical time step
   nsm::ElementLaunch  elaunch{128, 0, 0};
+  nsm_mlp*            closure = nullptr;        // learned material (FP32 form), or null
+  unsigned long long* d_fallbacks = nullptr;    // points that left the closure's envelope
 
   std::vector<BcLine> bcs;
   bool                bcs_dirty = true;
@@ -119,7 +122,7 @@ void free_all(nsm_model* m)
                   m->d_f,    m->d_fext,     m->d_mass,     m->d_inv_mass, m->d_geo,    m->d_ip,    m->d_Xf,
                   m->d_uf,   m->d_fe,   m->d_status,   m->d_step_base, m->d_scratch, m->d_stage,  m->d_out,   m->d_bc_slot,
                   m->d_bcs,  m->d_ibc_slot, m->d_ibcs,     m->d_sched, m->d_group_out, m->d_elem_group,
-                  m->d_node_group, m->d_elem_off, m->d_mats};
+                  m->d_node_group, m->d_elem_off, m->d_mats, m->d_fallbacks};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (auto& e : m->ev_elem) {
@@ -267,6 +270,12 @@ cudaError_t sync_uf(nsm_model* m)
 cudaError_t launch_element(nsm_model* m, int k)
 {
   nsm::ElementArgs a = element_args(m, k);
+  if (m->closure) {
+    nsm::mlp::MlpElementArgs ma;
+    nsm::mlp::element_args(m->closure, &ma, nullptr, nullptr);
+    ma.fallback_count = m->d_fallbacks;
+    return nsm::mlp::launch_element_mlp(a, ma, m->stream);
+  }
   return m->precision == NSM_PRECISION_FP64 ? nsm::launch_element_fp64(a, m->elaunch, m->stream)
                                             : nsm::launch_element_fp32(a, m->elaunch, m->stream);
 }
@@ -948,6 +957,38 @@ int nsm_autotune(nsm_model* m, int repeats, int* chosen, double* best_ms)
   if (chosen) *chosen = best;
   if (best_ms) *best_ms = best_t / repeats;
   return read_status(m);
+}
+
+int nsm_set_mlp_closure(nsm_model* m, nsm_mlp* closure)
+{
+  if (!m) return fail(NSM_ERR_INVALID_ARGUMENT, "null model");
+  if (closure) {
+    if (m->precision != NSM_PRECISION_FP32_MIXED) return fail(NSM_ERR_INVALID_ARGUMENT, "the learned closure runs in the FP32-mixed form");
+    if (m->S != 1) return fail(NSM_ERR_INVALID_ARGUMENT, "the learned closure is trained for one material");
+    double K = 0, G = 0;
+    nsm::mlp::MlpElementArgs ma;
+    nsm::mlp::element_args(closure, &ma, &K, &G);
+    if (K != m->K || G != m->G) return fail(NSM_ERR_INVALID_ARGUMENT, "closure trained for another material");
+  }
+  NSM_CUDA(cudaSetDevice(m->device));
+  if (!m->d_fallbacks) {
+    NSM_CUDA(cudaMalloc(&m->d_fallbacks, sizeof(unsigned long long)));
+    NSM_CUDA(cudaMemsetAsync(m->d_fallbacks, 0, sizeof(unsigned long long), m->stream));
+  }
+  m->closure = closure;
+  for (auto& g : m->graphs) cudaGraphExecDestroy(g.second);
+  m->graphs.clear();
+  return NSM_OK;
+}
+
+int nsm_closure_fallbacks(nsm_model* m, unsigned long long* count)
+{
+  if (!m || !count) return fail(NSM_ERR_INVALID_ARGUMENT, "null argument");
+  *count = 0;
+  if (!m->d_fallbacks) return NSM_OK;
+  NSM_CUDA(cudaMemcpyAsync(count, m->d_fallbacks, sizeof(unsigned long long), cudaMemcpyDeviceToHost, m->stream));
+  NSM_CUDA(cudaStreamSynchronize(m->stream));
+  return NSM_OK;
 }
 
 int nsm_launches_per_advance(nsm_model* m, int num_steps)

@@ -89,6 +89,18 @@ SIGNATURES = {
     "nsm_autotune": (C.c_int, [_vp, C.c_int, _ip, _dp]),
     "nsm_critical_time_step_noalloc": (C.c_int, [C.c_int, C.c_int, _vp, _vp, _vp, C.c_double, C.c_double, _vp,
                                                 _vp]),
+    "nsm_mlp_last_error": (C.c_char_p, []),
+    "nsm_mlp_create": (C.c_int, [C.c_double, C.c_double, C.c_ulonglong, C.c_int, C.POINTER(_vp)]),
+    "nsm_mlp_destroy": (C.c_int, [_vp]),
+    "nsm_mlp_generate": (C.c_int, [_vp, C.c_long, C.c_ulonglong, C.c_double, C.c_double]),
+    "nsm_mlp_train": (C.c_int, [_vp, C.c_int, C.c_int, C.c_double, _dp]),
+    "nsm_mlp_get_params": (C.c_int, [_vp, _dp_f, _dp_f]),
+    "nsm_mlp_set_params": (C.c_int, [_vp, _dp_f, _dp_f]),
+    "nsm_mlp_training_sample": (C.c_int, [_vp, C.c_long, C.c_long, _dp_f, _dp_f]),
+    "nsm_mlp_gradient": (C.c_int, [_vp, C.c_long, _dp_f, _dp_f, _dp_f, _dp]),
+    "nsm_mlp_predict": (C.c_int, [_vp, C.c_long, _dp, _dp, _ip]),
+    "nsm_set_mlp_closure": (C.c_int, [_vp, _vp]),
+    "nsm_closure_fallbacks": (C.c_int, [_vp, C.POINTER(C.c_ulonglong)]),
     "nsm_tc_selftest": (C.c_int, [C.c_int, C.c_int, _dp_f, _dp_f, _dp_f]),
     "nsm_host_alloc": (_vp, [C.c_size_t]),
     "nsm_host_free": (None, [_vp]),
@@ -262,6 +274,16 @@ class Model:
     def sample_slice(self, g):
         return slice(int(self.node_offsets[g]), int(self.node_offsets[g + 1]))
 
+    def set_closure(self, closure):
+        """Use a trained MLPClosure as the material (FP32-mixed form)."""
+        self._closure = closure
+        _check(library().nsm_set_mlp_closure(self._h, None if closure is None else closure._h))
+
+    def closure_fallbacks(self):
+        c = C.c_ulonglong()
+        _check(library().nsm_closure_fallbacks(self._h, C.byref(c)))
+        return c.value
+
     def autotune(self, repeats=5):
         c, ms = C.c_int(), C.c_double()
         _check(library().nsm_autotune(self._h, repeats, C.byref(c), C.byref(ms)))
@@ -315,6 +337,75 @@ class Model:
         _check(library().nsm_get_profile(self._h, C.byref(te), C.byref(ne), C.byref(tn), C.byref(nn)))
         return {"element_ms": te.value, "element_launches": ne.value, "node_ms": tn.value,
                 "node_launches": nn.value}
+
+
+def _check_mlp(rc):
+    if rc != NSM_OK:
+        raise EngineError(rc, library().nsm_mlp_last_error().decode())
+
+
+class MLPClosure:
+    """The learned constitutive closure (nsm_mlp_*): a BF16 tensor-core MLP
+    standing in for the neo-Hookean stress update."""
+
+    PARAMS = 5190
+
+    def __init__(self, bulk_modulus, shear_modulus, seed=1, device=0):
+        h = _vp()
+        _check_mlp(library().nsm_mlp_create(bulk_modulus, shear_modulus, seed, device, C.byref(h)))
+        self._h = h
+        self.bulk_modulus, self.shear_modulus = bulk_modulus, shear_modulus
+
+    def close(self):
+        if getattr(self, "_h", None):
+            library().nsm_mlp_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def generate(self, n, seed=7, perturbation=0.05, min_det=0.5):
+        _check_mlp(library().nsm_mlp_generate(self._h, int(n), seed, perturbation, min_det))
+
+    def train(self, epochs, batch_tiles=128, lr=2e-3):
+        loss = C.c_double()
+        _check_mlp(library().nsm_mlp_train(self._h, int(epochs), int(batch_tiles), lr, C.byref(loss)))
+        return loss.value
+
+    def params(self):
+        p = np.zeros(self.PARAMS, np.float32)
+        s = np.zeros(5, np.float32)
+        _check_mlp(library().nsm_mlp_get_params(self._h, p.ctypes.data_as(_dp_f), s.ctypes.data_as(_dp_f)))
+        return p, s
+
+    def set_params(self, params=None, scales=None):
+        p = None if params is None else np.ascontiguousarray(params, np.float32)
+        s = None if scales is None else np.ascontiguousarray(scales, np.float32)
+        _check_mlp(library().nsm_mlp_set_params(self._h, None if p is None else p.ctypes.data_as(_dp_f),
+                                                None if s is None else s.ctypes.data_as(_dp_f)))
+
+    def training_sample(self, first, count):
+        H = np.zeros((count, 9), np.float32)
+        Y = np.zeros((count, 6), np.float32)
+        _check_mlp(library().nsm_mlp_training_sample(self._h, first, count, H.ctypes.data_as(_dp_f),
+                                                     Y.ctypes.data_as(_dp_f)))
+        return H, Y
+
+    def gradient(self, H, Y):
+        H = np.ascontiguousarray(H, np.float32)
+        Y = np.ascontiguousarray(Y, np.float32)
+        g = np.zeros(self.PARAMS, np.float32)
+        loss = C.c_double()
+        _check_mlp(library().nsm_mlp_gradient(self._h, H.shape[0], H.ctypes.data_as(_dp_f), Y.ctypes.data_as(_dp_f),
+                                              g.ctypes.data_as(_dp_f), C.byref(loss)))
+        return g, loss.value
+
+    def predict(self, F):
+        F = np.ascontiguousarray(F, np.float64).reshape(-1, 9)
+        s = np.zeros((F.shape[0], 6))
+        fb = C.c_int()
+        _check_mlp(library().nsm_mlp_predict(self._h, F.shape[0], _d(F), _d(s), C.byref(fb)))
+        return s, fb.value
 
 
 def _concatenate(problems):

@@ -1,0 +1,102 @@
+"""CPU oracle of the learned closure's network (TEST INFRASTRUCTURE ONLY).
+
+The engine's MLP (nimblesm_gb300/csrc/mlp_common.cuh): sigma/G = L(H) +
+s_r * |x|^2 * MLP(x), x = H * s_in, MLP = 9 -> 64 -> 64 -> 6 with GELU, evaluated with BF16
+operands and FP32 accumulation on the tensor cores.  This module restates the
+forward pass and the gradient of the training loss in float64 numpy, either
+emulating the BF16 roundings at exactly the points where the GPU rounds
+(emulate=True, for a tight gradient check) or in exact arithmetic
+(emulate=False, the mathematical gradient).
+"""
+import numpy as np
+from scipy.special import erf
+
+HID, IN, OUT = 64, 9, 6
+oW1, ob1 = 0, HID * IN
+oW2, ob2 = ob1 + HID, ob1 + HID + HID * HID
+oW3, ob3 = ob2 + HID, ob2 + HID + OUT * HID
+NPARAMS = ob3 + OUT
+
+
+def bf16(x):
+    """Round to the nearest BF16 (ties to even), as float64."""
+    b = np.ascontiguousarray(x, dtype=np.float32).view(np.uint32).astype(np.uint64)
+    b = (b + 0x7FFF + ((b >> 16) & 1)) & 0xFFFF0000
+    return b.astype(np.uint32).view(np.float32).astype(np.float64)
+
+
+def unpack(P):
+    P = np.asarray(P, np.float64)
+    return (P[oW1:ob1].reshape(HID, IN), P[ob1:oW2], P[oW2:ob2].reshape(HID, HID), P[ob2:oW3],
+            P[oW3:ob3].reshape(OUT, HID), P[ob3:])
+
+
+def linear_part(H, k_over_g):
+    """Small-strain neo-Hookean stress over G (symmetric order), H row-major."""
+    tr = H[:, 0] + H[:, 4] + H[:, 8]
+    a, d = k_over_g * tr, tr / 3.0
+    return np.stack([a + 2 * (H[:, 0] - d), a + 2 * (H[:, 4] - d), a + 2 * (H[:, 8] - d),
+                     H[:, 1] + H[:, 3], H[:, 5] + H[:, 7], H[:, 6] + H[:, 2]], axis=1)
+
+
+def gelu(z):
+    return 0.5 * z * (1.0 + erf(z / np.sqrt(2.0)))
+
+
+def gelu_grad(z):
+    return 0.5 * (1.0 + erf(z / np.sqrt(2.0))) + z * np.exp(-0.5 * z * z) / np.sqrt(2.0 * np.pi)
+
+
+def forward(P, scales, H, emulate=True):
+    W1, b1, W2, b2, W3, b3 = unpack(P)
+    r = bf16 if emulate else (lambda v: np.asarray(v, np.float64))
+    xs = (np.asarray(H, np.float32) * np.float32(scales[0])).astype(np.float32)
+    hi = bf16(xs) if emulate else xs.astype(np.float64)
+    lo = bf16((xs - hi.astype(np.float32)).astype(np.float32)) if emulate else np.zeros_like(hi)
+    n = H.shape[0]
+    X = np.zeros((n, 32))
+    X[:, :9], X[:, 9], X[:, 16:25] = hi, 1.0, lo
+    W1x = np.zeros((HID, 32))
+    W1x[:, :9], W1x[:, 9], W1x[:, 16:25] = W1, b1, W1
+    z1 = X @ r(W1x).T
+    a1 = r(gelu(z1))
+    z2 = a1 @ r(W2).T + b2
+    a2 = r(gelu(z2))
+    out = a2 @ r(W3).T + b3
+    return dict(X=X, z1=z1, a1=a1, z2=z2, a2=a2, out=out)
+
+
+def gate(H, scales):
+    xs = (np.asarray(H, np.float32) * np.float32(scales[0])).astype(np.float64)
+    return np.maximum((xs * xs).sum(axis=1), 1e-12)
+
+
+def stress_over_g(P, scales, H, emulate=True):
+    f = forward(P, scales, H, emulate)
+    return linear_part(np.asarray(H, np.float64), scales[2]) + (scales[1] * gate(H, scales))[:, None] * f["out"]
+
+
+def loss_and_gradient(P, scales, H, Y, emulate=True):
+    """Mean over points of the squared scaled residual and its gradient."""
+    W1, b1, W2, b2, W3, b3 = unpack(P)
+    r = bf16 if emulate else (lambda v: np.asarray(v, np.float64))
+    n = H.shape[0]
+    f = forward(P, scales, H, emulate)
+    t = (np.asarray(Y, np.float64) - linear_part(np.asarray(H, np.float64), scales[2])) / \
+        (scales[1] * gate(H, scales))[:, None]
+    d = f["out"] - t
+    loss = float((d * d).sum() / n)
+    g = r(2.0 * d / n)
+    dW3, db3 = g.T @ f["a2"], g.sum(axis=0)
+    dz2 = r((g @ r(W3)) * gelu_grad(f["z2"]))
+    dW2, db2 = dz2.T @ f["a1"], dz2.sum(axis=0)
+    dz1 = r((dz2 @ r(W2)) * gelu_grad(f["z1"]))
+    dW1x = dz1.T @ f["X"]
+    grad = np.zeros(NPARAMS)
+    grad[oW1:ob1] = (dW1x[:, :9] + dW1x[:, 16:25]).ravel()
+    grad[ob1:oW2] = dW1x[:, 9]
+    grad[oW2:ob2] = dW2.ravel()
+    grad[ob2:oW3] = db2
+    grad[oW3:ob3] = dW3.ravel()
+    grad[ob3:] = db3
+    return loss, grad

@@ -1,0 +1,136 @@
+"""The learned constitutive closure: training data from the material, the
+tensor-core forward pass and loss gradient against the CPU oracle
+(oracle/mlp_oracle.py), and what training buys over the closure's linear
+part alone."""
+import numpy as np
+import pytest
+
+from nimblesm_gb300 import engine as E
+from oracle import mlp_oracle as M
+from oracle import oracle as O
+from tests.gpu_util import rel
+
+pytestmark = pytest.mark.gpu
+K, G = 160e9, 79.3e9
+
+
+@pytest.fixture(scope="module")
+def mlp():
+    from nimblesm_gb300 import build as B
+    B.build()
+    O.build(ref=False)
+    m = E.MLPClosure(K, G, seed=3)
+    m.generate(1 << 20, seed=11)
+    yield m
+    m.close()
+
+
+def to_reference_F(H):
+    slot = [0, 3, 8, 6, 1, 4, 5, 7, 2]  # row-major (i,J) -> reference full-tensor slot
+    F = np.zeros((H.shape[0], 9))
+    for q in range(9):
+        F[:, slot[q]] = H[:, q] + (1.0 if q % 4 == 0 else 0.0)
+    return F
+
+
+def test_training_pairs_are_the_material(mlp):
+    H, Y = mlp.training_sample(1000, 512)
+    assert np.abs(H).max() < 0.5 and 0.045 < H.std() < 0.055
+    sig = O.stress(to_reference_F(H.astype(np.float64)), K, G)  # the reference's arithmetic
+    assert rel(Y, sig / G) < 1e-6  # FP32 storage of the targets
+
+
+def test_forward_matches_oracle(mlp):
+    P, S = mlp.params()
+    rng = np.random.default_rng(0)
+    P = P + rng.normal(0, 0.05, P.shape).astype(np.float32)  # non-trivial biases too
+    mlp.set_params(P, S)
+    H, _ = mlp.training_sample(0, 2048)
+    sig, fb = mlp.predict(to_reference_F(H.astype(np.float64)))
+    inside = np.abs(H).max(axis=1) <= S[3]
+    ref = M.stress_over_g(P, S, H) * G
+    assert rel(sig[inside], ref[inside]) < 2e-3
+    assert fb == int((~inside).sum())
+
+
+def test_gradient_matches_oracle(mlp):
+    P, S = mlp.params()
+    rng = np.random.default_rng(1)
+    P = P + rng.normal(0, 0.05, P.shape).astype(np.float32)
+    mlp.set_params(P, S)
+    H, Y = mlp.training_sample(4096, 1024)
+    g, loss = mlp.gradient(H, Y)
+    l_e, g_e = M.loss_and_gradient(P, S, H, Y, emulate=True)
+    l_x, g_x = M.loss_and_gradient(P, S, H, Y, emulate=False)
+    assert abs(loss - l_e) < 1e-3 * l_e
+    assert rel(g, g_e) < 2e-2          # same BF16 rounding points as the GPU
+    assert rel(g, g_x) < 5e-2          # the exact mathematical gradient, to BF16 precision
+    for lo, hi in ((M.oW1, M.ob1), (M.oW2, M.ob2), (M.oW3, M.ob3)):
+        assert rel(g[lo:hi], g_e[lo:hi]) < 3e-2
+
+
+def test_training_gains_over_the_linear_part(mlp):
+    mlp.set_params(E.MLPClosure(K, G, seed=3).params()[0])  # fresh weights, keep the data's scales
+    loss = mlp.train(epochs=40, batch_tiles=16, lr=5e-3)
+    P, S = mlp.params()
+    rng = np.random.default_rng(99)
+    H = rng.normal(0, 0.05, size=(4096, 9))
+    F = to_reference_F(H)
+    exact = O.stress(F, K, G) / G
+    sig, fb = mlp.predict(F)
+    inside = np.abs(H).max(axis=1) <= S[3]
+    lin = M.linear_part(H, S[2])
+    e_mlp = rel(sig[inside] / G, exact[inside])
+    e_lin = rel(lin[inside], exact[inside])
+    print(f"loss {loss:.3e}  stress error: linear part {e_lin:.3e}, with the trained network {e_mlp:.3e}")
+    assert loss < 0.05
+    assert e_mlp < 0.05 * e_lin, (e_mlp, e_lin)
+
+
+def test_fused_element_kernel_matches_predict(mlp):
+    """The closure inside the element kernel computes the same stress as the
+    standalone inference of the same points."""
+    from nimblesm_gb300.mesh import cube_problem
+    p = cube_problem(6, jitter=0.2, seed=4)
+    m = E.Model(p, precision="fp32")
+    m.set_closure(mlp)
+    rng = np.random.default_rng(5)
+    m.SetVectorNodeData("displacement", rng.normal(0, 2e-3, size=(p.num_nodes, 3)))
+    m.ComputeInternalForce()
+    F, sig = m.GetIntegrationPointData()
+    ref, fb = mlp.predict(F.reshape(-1, 9))
+    assert rel(sig.reshape(-1, 6), ref) < 1e-5
+    assert m.closure_fallbacks() == fb
+
+
+def test_small_strain_limit(mlp):
+    """The gated closure reduces to the material's small-strain response: at
+    strains of 1e-4 its stress error is far below the linear part's own
+    O(|H|) model error of the neo-Hookean material, not a network error floor."""
+    P, S = mlp.params()
+    rng = np.random.default_rng(7)
+    H = rng.normal(0, 1e-4, size=(2048, 9))
+    F = to_reference_F(H)
+    exact = O.stress(F, K, G) / G
+    sig, fb = mlp.predict(F)
+    assert fb == 0
+    assert rel(sig / G, exact) < 1e-3
+
+
+def test_explicit_run_with_the_closure(mlp):
+    """An explicit run whose material is the trained network, against the FP64
+    plain run: displacement error, and no envelope fallbacks at these strains."""
+    from nimblesm_gb300.mesh import cube_problem, critical_time_step
+    p = cube_problem(16, jitter=0.2, seed=2)
+    dt = 0.5 * critical_time_step(p)
+    steps = 400
+    ref = E.run(p, steps * dt, steps, precision="fp64")
+    m = E.Model(p, precision="fp32")
+    m.set_closure(mlp)
+    m.begin(steps * dt, steps, 0)
+    m.advance(steps)
+    st = m.state(with_ip=False)
+    e = rel(st["u"], ref["u"])
+    print(f"closure run: relative displacement error {e:.3e} after {steps} steps, fallbacks {m.closure_fallbacks()}")
+    assert e < 1e-3
+    assert m.closure_fallbacks() == 0

@@ -52,10 +52,78 @@ struct Scales {
   float min_det;    // det F bound of the training envelope
 };
 
-__device__ __forceinline__ float gelu(float z) { return 0.5f * z * (1.0f + erff(z * 0.70710678118654752f)); }
+// GELU in its tanh form, 0.5 z (1 + tanh(c (z + 0.044715 z^3))),
+// c = sqrt(2/pi) (Hendrycks & Gimpel 2016), on the hardware tanh
+// (tanh.approx.f32, relative error about 2^-11, below the BF16 rounding of
+// the activations it produces).  Training, inference and the CPU oracle all
+// use this form.
+constexpr float kGeluC = 0.7978845608028654f, kGeluCB = 0.7978845608028654f * 0.044715f;
+
+__device__ __forceinline__ float tanh_approx(float u)
+{
+  float t;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(u));
+  return t;
+}
+__device__ __forceinline__ float gelu(float z)
+{
+  const float t  = tanh_approx(z * fmaf(kGeluCB, z * z, kGeluC));
+  const float hz = 0.5f * z;
+  return fmaf(hz, t, hz);
+}
 __device__ __forceinline__ float gelu_grad(float z)
 {
-  return 0.5f * (1.0f + erff(z * 0.70710678118654752f)) + z * 0.39894228040143268f * __expf(-0.5f * z * z);
+  const float z2 = z * z;
+  const float t  = tanh_approx(z * fmaf(kGeluCB, z2, kGeluC));
+  const float du = fmaf(3.0f * kGeluCB, z2, kGeluC);
+  return 0.5f * (1.0f + t) + 0.5f * z * (1.0f - t * t) * du;
+}
+
+// ---- packed FP32x2 arithmetic (add/mul/fma .rn.f32x2, sm_100 and later) ----
+// Each lane is the IEEE round-to-nearest FP32 operation, so a packed
+// evaluation is bitwise the scalar one in the same order.
+using f32x2 = unsigned long long;
+__device__ __forceinline__ f32x2 f2_pack(float x, float y)
+{
+  f32x2 r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(x), "f"(y));
+  return r;
+}
+__device__ __forceinline__ void f2_unpack(f32x2 v, float& x, float& y) { asm("mov.b64 {%0, %1}, %2;" : "=f"(x), "=f"(y) : "l"(v)); }
+__device__ __forceinline__ f32x2 f2_add(f32x2 a, f32x2 b)
+{
+  f32x2 d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f32x2 f2_mul(f32x2 a, f32x2 b)
+{
+  f32x2 d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f32x2 f2_fma(f32x2 a, f32x2 b, f32x2 c)
+{
+  f32x2 d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+
+// Twice the GELU of two pre-activations, z + z tanh(u), packed to a BF16
+// pair (low half = first value).  Scaling by 2 commutes with every rounding
+// here, so this is exactly 2 * gelu() of each lane, and a next layer whose
+// weights are halved (also exact in BF16) computes bitwise what the
+// unscaled network computes, with one multiply per pair fewer.
+__device__ __forceinline__ uint32_t gelu_twice_bf16(f32x2 z)
+{
+  const f32x2 z2 = f2_mul(z, z);
+  const f32x2 in = f2_fma(f2_pack(kGeluCB, kGeluCB), z2, f2_pack(kGeluC, kGeluC));
+  float       u0, u1;
+  f2_unpack(f2_mul(z, in), u0, u1);
+  float g0, g1;
+  f2_unpack(f2_fma(z, f2_pack(tanh_approx(u0), tanh_approx(u1)), z), g0, g1);
+  __nv_bfloat162 b = __floats2bfloat162_rn(g0, g1);
+  return *reinterpret_cast<uint32_t*>(&b);
 }
 
 // Small-strain limit of the neo-Hookean stress over G, symmetric order.

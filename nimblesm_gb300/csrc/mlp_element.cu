@@ -1,14 +1,23 @@
 // Element kernel with the learned closure as the material update: the FP32
-// element kernel (element_kernels.cu) with the neo-Hookean stress replaced
-// by the MLP of mlp_common.cuh, evaluated on the 5th-generation tensor cores
+// element work (element_kernels.cu) with the neo-Hookean stress replaced by
+// the MLP of mlp_common.cuh, evaluated on the 5th-generation tensor cores
 // inside the element kernel.
 //
-// One CTA = 128 elements (thread r owns element r) = 8 tiles of 128 points,
-// tile p holding integration point p of every element.  Row r of a tile is
-// thread r's point, so each layer's accumulator row comes back to the thread
-// that owns the element (tensor-memory lane r) with no data exchange.  Points
-// outside the training envelope take the plain neo-Hookean stress (FP32) and
-// are counted.
+// One thread per integration point.  A CTA of 128 threads holds 16 elements
+// x 8 points (thread r = 8 * element + point), so one 128-row tile of points
+// per network layer, and accumulator row r (tensor-memory lane r) comes back
+// to the thread that owns point r.  A warp holds 4 whole elements, so all
+// element-level exchange stays inside the warp:
+//   * gather: thread (element, p) loads node p of its element and stages it
+//     in shared memory; each thread then reads the element's 8 nodes;
+//   * B^T sigma: each thread forms its point's contribution to the 24 nodal
+//     forces, and a 3-level butterfly over the element's 8 lanes leaves lane
+//     p with the sum for node p (21 shuffles, no shared memory).
+// The CTAs are persistent: each loads the operand images once and walks
+// chunks of 16 elements.  The three layers use the same 64 tensor-memory
+// columns in turn, so up to 8 CTAs fit the 512 columns of an SM.
+// Points outside the training envelope take the plain neo-Hookean stress
+// (FP32) and are counted.
 #include <cuda_runtime.h>
 
 #include "hex_math.cuh"
@@ -22,41 +31,37 @@ namespace mlp {
 using namespace tc;
 
 namespace el {
-constexpr int X    = 0;                    // [128][32]
-constexpr int A1   = X + 128 * kInX * 2;   // [128][64]
-constexpr int A2   = A1 + 128 * kHid * 2;  // [128][64]
-constexpr int W    = A2 + 128 * kHid * 2;  // W1x, W2, W3x images
-constexpr int B    = W + kOffW2t;          // b2[64], b3[6]
-constexpr int END  = B + 512;
-constexpr int SMEM = END + 16384;
-// Z1 and Z3 share columns (Z1 is consumed before layer 3 writes)
-constexpr uint32_t cZ1 = 0, cZ2 = 64, cZ3 = 0, kCols = 128;
+// A: [128][64] activations; the layer-1 input X [128][32] uses its first
+// 8 KB, and the per-warp node staging (4 elements x 8 nodes x 32 B) sits in
+// the warp's own X rows (bytes [2048 w, 2048 w + 1024)).
+constexpr int A    = 0;
+constexpr int W    = A + 128 * kHid * 2;  // W1x, W2, W3x images
+constexpr int B    = W + kOffW2t;         // b2[64], b3[6]
+constexpr int SMEM = B + 512;
+constexpr int kStageWarp = 2048;          // bytes between the warps' staging areas
+constexpr uint32_t kCols = 64;
+constexpr int kElems = 16;                // elements per chunk
 }  // namespace el
 
-__device__ __forceinline__ void publish()
+// Make this CTA's operand writes visible to the tensor core and order them
+// before the MMAs thread 0 is about to issue; false if any thread has
+// recorded a timed-out wait (the whole CTA then leaves its loop together).
+__device__ __forceinline__ bool publish(const int* err)
 {
   fence_proxy_async();
-  fence_before_sync();
-  __syncthreads();
-  fence_after_sync();
-}
-
-__device__ __forceinline__ bool wait_commit(uint64_t* mbar, uint32_t& phase, int* err)
-{
-  const bool ok = mbar_wait(mbar, phase);
-  phase ^= 1u;
-  if (!ok) atomicOr(err, 1);
   fence_before_sync();
   __syncthreads();
   fence_after_sync();
   return *err == 0;
 }
 
-__device__ __forceinline__ void ld_cols(uint32_t tb, uint32_t col, int n16, float* v)
+// Each thread waits for the commit itself (no block barrier): a timeout is
+// recorded and acted on at the next publish().
+__device__ __forceinline__ void wait_commit(uint64_t* mbar, uint32_t& phase, int* err)
 {
-  const uint32_t lane_base = (uint32_t)((threadIdx.x >> 5) * 32) << 16;
-  for (int c = 0; c < n16; c++) tmem_ld16(tb + lane_base + col + 16 * c, v + 16 * c);
-  tmem_wait_ld();
+  if (!mbar_wait(mbar, phase)) atomicOr(err, 1);
+  phase ^= 1u;
+  fence_after_sync();
 }
 
 __device__ __forceinline__ void layer(uint32_t d, const uint8_t* a, int Ka, const uint8_t* b, int N)
@@ -67,15 +72,76 @@ __device__ __forceinline__ void layer(uint32_t d, const uint8_t* a, int Ka, cons
              idesc, ks > 0);
 }
 
+// Hidden-layer epilogue: 64 accumulator columns of this thread's row ->
+// 2 GELU(z + bias) -> BF16 row r of the [128][64] activation tile, two
+// columns per packed FP32x2 operation (the next layer's weights are halved).
+__device__ __forceinline__ void hidden_epilogue(uint32_t taddr, const float* bias, uint8_t* tile, int r)
+{
+#pragma unroll
+  for (int h = 0; h < 4; h++) {
+    float z[16];
+    tmem_ld16(taddr + 16 * h, z);
+    tmem_wait_ld();
+#pragma unroll
+    for (int k0 = 0; k0 < 16; k0 += 8) {
+      uint32_t w[4];
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        f32x2 v = f2_pack(z[k0 + 2 * j], z[k0 + 2 * j + 1]);
+        if (bias) v = f2_add(v, *reinterpret_cast<const f32x2*>(bias + 16 * h + k0 + 2 * j));
+        w[j] = gelu_twice_bf16(v);
+      }
+      *reinterpret_cast<uint4*>(tile + kmajor_offset(r, 16 * h + k0, kHid)) = make_uint4(w[0], w[1], w[2], w[3]);
+    }
+  }
+}
+
+// Derivative weights of this thread's point: dN_n/dxi_d at point p is
+// sgn_d(n) * w[d][b][c] with (b, c) the corner's sign bits along the two
+// other axes: w = (b == s ? 1+g : 1-g) * (c == t ? (1+g)/8 : (1-g)/8),
+// (s, t) the point's sign bits along those axes (the 2-point transforms of
+// hex_math.cuh, evaluated at one point).
+__device__ __forceinline__ void point_weights(int p, float w[3][2][2])
+{
+  using Wt         = Weights<float>;
+  const int bit[3] = {sx_of(p), sy_of(p), sz_of(p)};
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    const int s = bit[other1(d)], t = bit[other2(d)];
+#pragma unroll
+    for (int b = 0; b < 2; b++)
+#pragma unroll
+      for (int c = 0; c < 2; c++) w[d][b][c] = (b == s ? Wt::wp : Wt::wm) * (c == t ? Wt::c1 : Wt::c2);
+  }
+}
+
+// dx_i/dxi_d at the point: D[i][d].
+__device__ __forceinline__ void point_gradient(const float x[8][3], const float w[3][2][2], float D[3][3])
+{
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    const int o1 = other1(d), o2 = other2(d);
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      float v = 0.0f;
+#pragma unroll
+      for (int b = 0; b < 2; b++)
+#pragma unroll
+        for (int c = 0; c < 2; c++)
+          v = fmaf(w[d][b][c], x[corner_axes(d, 1, o1, b, o2, c)][i] - x[corner_axes(d, 0, o1, b, o2, c)][i], v);
+      D[i][d] = v;
+    }
+  }
+}
+
 __global__ void __launch_bounds__(128) k_element_mlp(ElementArgs a, MlpElementArgs m)
 {
   extern __shared__ __align__(1024) uint8_t sm[];
   __shared__ uint64_t mbar;
   __shared__ uint32_t tslot;
   __shared__ int      err;
-  const int           r = threadIdx.x, warp = r >> 5;
-  const int           e = blockIdx.x * 128 + r;
-  const bool          valid = e < a.E;
+  const int           r = threadIdx.x, warp = r >> 5, lane = r & 31;
+  const int           p = r & 7, el = r >> 3;
   const long          ld_e = a.ld_e, ld_n = a.ld_n;
 
   if (warp == 0) {
@@ -87,114 +153,154 @@ __global__ void __launch_bounds__(128) k_element_mlp(ElementArgs a, MlpElementAr
     err = 0;
   }
   {
+    // W1x as is; W2 and W3x halved (exact in BF16), for the doubled activations
     const uint4* src = reinterpret_cast<const uint4*>(m.img);
-    for (int i = r; i < kOffW2t / 16; i += 128) reinterpret_cast<uint4*>(sm + el::W)[i] = src[i];
+    for (int i = r; i < kOffW2t / 16; i += 128) {
+      uint4 v = src[i];
+      if (i >= kOffW2 / 16) {
+        const __nv_bfloat162 half2 = __floats2bfloat162_rn(0.5f, 0.5f);
+        uint32_t*            q     = reinterpret_cast<uint32_t*>(&v);
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+          __nv_bfloat162 h = __hmul2(*reinterpret_cast<__nv_bfloat162*>(&q[j]), half2);
+          q[j]             = *reinterpret_cast<uint32_t*>(&h);
+        }
+      }
+      reinterpret_cast<uint4*>(sm + el::W)[i] = v;
+    }
     float* bias = reinterpret_cast<float*>(sm + el::B);
     if (r < kHid) bias[r] = m.P[ob2 + r];
     if (r < kOut) bias[64 + r] = m.P[ob3 + r];
   }
-  const float* b2 = reinterpret_cast<const float*>(sm + el::B);
-  const float* b3 = b2 + 64;
-
-  // gradients of u and X at the points (as the FP32 element kernel)
-  float Gu[3][3][2][2], GX[3][3][2][2];
-  {
-    float xu[8][3], xX[8][3];
-    for (int n = 0; n < 8; n++) {
-      const int id = valid ? __ldg(&a.conn[n * ld_e + e]) : 0;
-      for (int k = 0; k < 3; k++) {
-        xu[n][k] = valid ? __ldg(&a.uf[k * ld_n + id]) : 0.0f;
-        xX[n][k] = valid ? __ldg(&a.Xf[k * ld_n + id]) : float(sign_bit(n, k));  // a unit cube for idle rows
-      }
-    }
-    nodal_gradient<float>(xu, Gu);
-    nodal_gradient<float>(xX, GX);
-  }
-  float S[3][3][2][2];
-  for (int d = 0; d < 3; d++)
-    for (int i = 0; i < 3; i++)
-      for (int s = 0; s < 2; s++)
-        for (int t = 0; t < 2; t++) S[d][i][s][t] = 0.0f;
-
-  const bool     store = a.store_ip || (a.sched != nullptr && a.sched[(long)(*a.step_base + a.k) * a.num_groups].is_output);
-  float*         rec   = reinterpret_cast<float*>(a.ip) + (size_t)e * kIpRecord;
+  fence_before_sync();
+  __syncthreads();
+  fence_after_sync();
+  const float*   b2    = reinterpret_cast<const float*>(sm + el::B);
+  const float*   b3    = b2 + 64;
   const uint32_t tb    = tslot;
-  uint32_t       phase = 0;
-  bool           bad = false;
-  int            fallbacks = 0;
+  const uint32_t taddr = tb + ((uint32_t)(warp * 32) << 16);
+  uint8_t* const stage = sm + el::A + warp * el::kStageWarp;
+  const bool     store = a.store_ip || (a.sched != nullptr && a.sched[(long)(*a.step_base + a.k) * a.num_groups].is_output);
   const float    K = (float)a.bulk, Gm = (float)a.shear;
+  float          w[3][2][2];
+  point_weights(p, w);
+  uint32_t phase     = 0;
+  int      fallbacks = 0;
+  int      status    = 0;
 
-  for (int p = 0; p < 8; p++) {
-    const int bit[3] = {sx_of(p), sy_of(p), sz_of(p)};
-    float     JX[3][3], G0[3][3], det0;
-    for (int i = 0; i < 3; i++)
-      for (int d = 0; d < 3; d++) JX[i][d] = GX[d][i][bit[other1(d)]][bit[other2(d)]];
-    invert3<float>(JX, G0, det0);
-    float H[3][3], h[9];
-    for (int i = 0; i < 3; i++)
-      for (int J = 0; J < 3; J++) {
-        float v = 0.0f;
-        for (int d = 0; d < 3; d++) v += Gu[d][i][bit[other1(d)]][bit[other2(d)]] * G0[d][J];
-        H[i][J]       = v;
-        h[3 * i + J] = v;
+  // The gather is software-pipelined one chunk ahead: the next chunk's node
+  // id is loaded while layer 1 runs and its coordinates while layer 2 runs.
+  const long nchunks = (a.E + el::kElems - 1) / el::kElems;
+  auto node_of = [&](long c) -> int {
+    const long e = c * el::kElems + el;
+    return (c < nchunks && e < a.E) ? __ldg(&a.conn[p * ld_e + e]) : -1;
+  };
+  auto values_of = [&](int id, float4& v0, float4& v1) {
+    if (id >= 0) {
+      v0 = make_float4(__ldg(&a.uf[id]), __ldg(&a.uf[ld_n + id]), __ldg(&a.uf[2 * ld_n + id]), __ldg(&a.Xf[id]));
+      v1 = make_float4(__ldg(&a.Xf[ld_n + id]), __ldg(&a.Xf[2 * ld_n + id]), 0.0f, 0.0f);
+    } else {  // idle rows: zero displacement on a unit cube
+      v0 = make_float4(0.0f, 0.0f, 0.0f, (float)sx_of(p));
+      v1 = make_float4((float)sy_of(p), (float)sz_of(p), 0.0f, 0.0f);
+    }
+  };
+  int    id_next = node_of(blockIdx.x);
+  float4 nv0, nv1;
+  values_of(id_next, nv0, nv1);
+  for (long chunk = blockIdx.x; chunk < nchunks; chunk += gridDim.x) {
+    const long e     = chunk * el::kElems + el;
+    const bool valid = e < a.E;
+
+    // ---- gather: node p of the element, staged for the element's 8 lanes ----
+    {
+      float4* st = reinterpret_cast<float4*>(stage + (lane >> 3) * 256 + p * 32);
+      st[0]      = nv0;
+      st[1]      = nv1;
+    }
+    __syncwarp();
+    float Du[3][3], DX[3][3];
+    {
+      float         xu[8][3], xX[8][3];
+      const float4* st = reinterpret_cast<const float4*>(stage + (lane >> 3) * 256);
+#pragma unroll
+      for (int n = 0; n < 8; n++) {
+        const float4 v0 = st[2 * n], v1 = st[2 * n + 1];
+        xu[n][0] = v0.x, xu[n][1] = v0.y, xu[n][2] = v0.z;
+        xX[n][0] = v0.w, xX[n][1] = v1.x, xX[n][2] = v1.y;
       }
-    // ---- MLP: layer 1 ----
+      point_gradient(xu, w, Du);
+      point_gradient(xX, w, DX);
+    }
+    __syncwarp();  // the staging area is overwritten by this warp's input rows below
+
+    float G0[3][3], det0, h[9];
+    invert3<float>(DX, G0, det0);
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int J = 0; J < 3; J++) h[3 * i + J] = Du[i][0] * G0[0][J] + Du[i][1] * G0[1][J] + Du[i][2] * G0[2][J];
+
+    // ---- layer 1: input row -> Z1 ----
     {
       float xs[9], row[kInX];
+#pragma unroll
       for (int q = 0; q < 9; q++) xs[q] = h[q] * m.sc.in_scale;
       input_row(xs, row);
-      for (int k0 = 0; k0 < kInX; k0 += 8) store_chunk(sm + el::X, r, k0, kInX, row + k0);
+#pragma unroll
+      for (int k0 = 0; k0 < kInX; k0 += 8) store_chunk(sm + el::A, r, k0, kInX, row + k0);
     }
-    publish();
+    if (!publish(&err)) break;
     if (r == 0) {
-      layer(tb + el::cZ1, sm + el::X, kInX, sm + el::W + kOffW1, kHid);
+      layer(tb, sm + el::A, kInX, sm + el::W + kOffW1, kHid);
       mma_commit(&mbar);
     }
-    if (!wait_commit(&mbar, phase, &err)) break;
-    {
-      float z[64];
-      ld_cols(tb, el::cZ1, 4, z);
-      for (int q = 0; q < 64; q++) z[q] = gelu(z[q]);
-      for (int k0 = 0; k0 < 64; k0 += 8) store_chunk(sm + el::A1, r, k0, kHid, z + k0);
-    }
-    publish();
+    id_next = node_of(chunk + gridDim.x);
+    wait_commit(&mbar, phase, &err);
+    hidden_epilogue(taddr, nullptr, sm + el::A, r);
+    // ---- layer 2 ----
+    if (!publish(&err)) break;
     if (r == 0) {
-      layer(tb + el::cZ2, sm + el::A1, kHid, sm + el::W + kOffW2, kHid);
+      layer(tb, sm + el::A, kHid, sm + el::W + kOffW2, kHid);
       mma_commit(&mbar);
     }
-    if (!wait_commit(&mbar, phase, &err)) break;
-    {
-      float z[64];
-      ld_cols(tb, el::cZ2, 4, z);
-      for (int q = 0; q < 64; q++) z[q] = gelu(z[q] + b2[q]);
-      for (int k0 = 0; k0 < 64; k0 += 8) store_chunk(sm + el::A2, r, k0, kHid, z + k0);
-    }
-    publish();
+    values_of(id_next, nv0, nv1);
+    wait_commit(&mbar, phase, &err);
+    hidden_epilogue(taddr, b2, sm + el::A, r);
+    // ---- layer 3 ----
+    if (!publish(&err)) break;
     if (r == 0) {
-      layer(tb + el::cZ3, sm + el::A2, kHid, sm + el::W + kOffW3, kOutX);
+      layer(tb, sm + el::A, kHid, sm + el::W + kOffW3, kOutX);
       mma_commit(&mbar);
     }
-    if (!wait_commit(&mbar, phase, &err)) break;
+    wait_commit(&mbar, phase, &err);
     float sig[6];
     {
       float z[16];
-      ld_cols(tb, el::cZ3, 1, z);
+      tmem_ld16(taddr, z);
+      tmem_wait_ld();
       if (in_envelope(h, m.sc)) {
         float L[6], xs[9];
+#pragma unroll
         for (int q = 0; q < 9; q++) xs[q] = h[q] * m.sc.in_scale;
         linear_part(h, m.sc.k_over_g, L);
         const float g = gate(xs) * m.sc.res_scale;
+#pragma unroll
         for (int q = 0; q < 6; q++) sig[q] = Gm * (L[q] + g * (z[q] + b3[q]));
       } else {
-        float C[3][3], J;
+        float H[3][3], C[3][3], J;
+#pragma unroll
+        for (int q = 0; q < 9; q++) H[q / 3][q % 3] = h[q];
         neohookean<float>(H, K, Gm, sig, C, J);
         fallbacks += valid ? 1 : 0;
       }
     }
-    // ---- the rest of the element work, as the FP32 element kernel ----
+
+    // ---- the point's share of B^T sigma (first Piola-Kirchhoff form) ----
     float F[3][3], C[3][3];
+#pragma unroll
     for (int i = 0; i < 3; i++)
-      for (int k = 0; k < 3; k++) F[i][k] = (i == k ? 1.0f : 0.0f) + H[i][k];
+#pragma unroll
+      for (int k = 0; k < 3; k++) F[i][k] = (i == k ? 1.0f : 0.0f) + h[3 * i + k];
     C[0][0] = F[1][1] * F[2][2] - F[1][2] * F[2][1];
     C[0][1] = F[1][2] * F[2][0] - F[1][0] * F[2][2];
     C[0][2] = F[1][0] * F[2][1] - F[1][1] * F[2][0];
@@ -205,67 +311,129 @@ __global__ void __launch_bounds__(128) k_element_mlp(ElementArgs a, MlpElementAr
     C[2][1] = F[0][2] * F[1][0] - F[0][0] * F[1][2];
     C[2][2] = F[0][0] * F[1][1] - F[0][1] * F[1][0];
     const float J = F[0][0] * C[0][0] + F[0][1] * C[0][1] + F[0][2] * C[0][2];
-    if (valid && (!(J > 0.0f) || !(det0 > 0.0f))) bad = true;
+    if (valid && (!(J > 0.0f) || !(det0 > 0.0f))) status |= NSM_STATUS_BAD_JACOBIAN;
     if (valid && store) {
       float rr[kIpRecord];
+#pragma unroll
       for (int i = 0; i < 3; i++)
+#pragma unroll
         for (int k = 0; k < 3; k++) rr[full_slot(i, k)] = F[i][k];
+#pragma unroll
       for (int q = 0; q < 6; q++) rr[9 + q] = sig[q];
-      rr[15] = 0.0f;
-      float* dst = rec + (size_t)p * ld_e * kIpRecord;
+      rr[15]     = 0.0f;
+      float* dst = reinterpret_cast<float*>(a.ip) + ((size_t)p * ld_e + e) * kIpRecord;
+#pragma unroll
       for (int k = 0; k < kIpRecord; k += 4) *reinterpret_cast<float4*>(dst + k) = make_float4(rr[k], rr[k + 1], rr[k + 2], rr[k + 3]);
     }
-    float P[3][3];
-    for (int i = 0; i < 3; i++)
-      for (int Jc = 0; Jc < 3; Jc++)
-        P[i][Jc] = sig[sym_slot(i, 0)] * C[0][Jc] + sig[sym_slot(i, 1)] * C[1][Jc] + sig[sym_slot(i, 2)] * C[2][Jc];
-    for (int d = 0; d < 3; d++)
-      for (int i = 0; i < 3; i++) {
-        const float q = G0[d][0] * P[i][0] + G0[d][1] * P[i][1] + G0[d][2] * P[i][2];
-        S[d][i][bit[other1(d)]][bit[other2(d)]] += det0 * q;
-      }
-  }
-  if (err == 0 && valid) {
-    float f[8][3];
-    for (int n = 0; n < 8; n++)
-      for (int i = 0; i < 3; i++) f[n][i] = 0.0f;
-    for (int d = 0; d < 3; d++) {
-      const int o1 = other1(d), o2 = other2(d);
-      for (int i = 0; i < 3; i++) {
-        float R[2][2];
-        bwd_transform<float>(S[d][i], R);
-        for (int b = 0; b < 2; b++)
-          for (int c = 0; c < 2; c++) {
-            f[corner_axes(d, 1, o1, b, o2, c)][i] -= R[b][c];
-            f[corner_axes(d, 0, o1, b, o2, c)][i] += R[b][c];
-          }
-      }
+    float S[3][3];  // S[d][i] = det0 sum_J G0[d][J] P[i][J],  P = sigma cof(F)
+    {
+      float P[3][3];
+#pragma unroll
+      for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int Jc = 0; Jc < 3; Jc++)
+          P[i][Jc] = sig[sym_slot(i, 0)] * C[0][Jc] + sig[sym_slot(i, 1)] * C[1][Jc] + sig[sym_slot(i, 2)] * C[2][Jc];
+#pragma unroll
+      for (int d = 0; d < 3; d++)
+#pragma unroll
+        for (int i = 0; i < 3; i++) S[d][i] = det0 * (G0[d][0] * P[i][0] + G0[d][1] * P[i][1] + G0[d][2] * P[i][2]);
     }
-    float* fo     = reinterpret_cast<float*>(a.fe) + (size_t)e * 24;
-    bool   finite = true;
+    // contribution to node n: -sum_d dN_n/dxi_d(p) S[d][i]
+    float f[8][3];
+#pragma unroll
     for (int n = 0; n < 8; n++)
-      for (int i = 0; i < 3; i++) finite = finite && isfinite(f[n][i]);
-    for (int k = 0; k < 24; k += 4)
-      *reinterpret_cast<float4*>(fo + k) = make_float4(f[k / 3][k % 3], f[(k + 1) / 3][(k + 1) % 3],
-                                                       f[(k + 2) / 3][(k + 2) % 3], f[(k + 3) / 3][(k + 3) % 3]);
-    if (bad || !finite) atomicOr(a.status, (bad ? NSM_STATUS_BAD_JACOBIAN : 0) | (finite ? 0 : NSM_STATUS_NONFINITE));
+#pragma unroll
+      for (int i = 0; i < 3; i++) {
+        float v = 0.0f;
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+          const float wd = w[d][sign_bit(n, other1(d))][sign_bit(n, other2(d))];
+          v              = sign_bit(n, d) ? fmaf(-wd, S[d][i], v) : fmaf(wd, S[d][i], v);
+        }
+        f[n][i] = v;
+      }
+    // butterfly over the element's 8 lanes: lane p ends with node p's sum
+    float      g4[4][3], g2[2][3], g1[3];
+    const bool hi4 = (p >> 2) & 1, hi2 = (p >> 1) & 1, hi1 = p & 1;
+#pragma unroll
+    for (int q = 0; q < 4; q++)
+#pragma unroll
+      for (int i = 0; i < 3; i++) {
+        const float keep = hi4 ? f[4 + q][i] : f[q][i], send = hi4 ? f[q][i] : f[4 + q][i];
+        g4[q][i]         = keep + __shfl_xor_sync(0xffffffffu, send, 4);
+      }
+#pragma unroll
+    for (int q = 0; q < 2; q++)
+#pragma unroll
+      for (int i = 0; i < 3; i++) {
+        const float keep = hi2 ? g4[2 + q][i] : g4[q][i], send = hi2 ? g4[q][i] : g4[2 + q][i];
+        g2[q][i]         = keep + __shfl_xor_sync(0xffffffffu, send, 2);
+      }
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      const float keep = hi1 ? g2[1][i] : g2[0][i], send = hi1 ? g2[0][i] : g2[1][i];
+      g1[i]            = keep + __shfl_xor_sync(0xffffffffu, send, 1);
+    }
+    if (valid) {
+      float* fo = reinterpret_cast<float*>(a.fe) + (size_t)e * 24 + 3 * p;
+      fo[0]     = g1[0];
+      fo[1]     = g1[1];
+      fo[2]     = g1[2];
+      if (!isfinite(g1[0]) || !isfinite(g1[1]) || !isfinite(g1[2])) status |= NSM_STATUS_NONFINITE;
+    }
   }
+  if (status) atomicOr(a.status, status);
   if (fallbacks) atomicAdd(m.fallback_count, (unsigned long long)fallbacks);
-  if (r == 0 && err) atomicOr(a.status, NSM_STATUS_TIMEOUT);
   fence_before_sync();
+  __syncthreads();  // every thread's timeout record is in `err`
+  if (r == 0 && err) {
+    mbar_wait(&mbar, phase ^ 1u);  // bounded: let the timed-out MMA drain before the columns are freed
+    atomicOr(a.status, NSM_STATUS_TIMEOUT);
+  }
   __syncthreads();
   if (warp == 0) tmem_dealloc(tb, el::kCols);
 }
 
+static int g_blocks_per_sm = 0;
+
+// Co-resident CTAs per SM from the kernel's registers and shared memory and
+// the device's limits, capped by the SM's 512 tensor-memory columns.  (The
+// runtime's occupancy query answers 1 for this kernel, which would leave a
+// single 4-warp CTA per SM.)  The CTAs never wait on one another, so a
+// count above what the hardware co-schedules only adds a wave.
 cudaError_t setup_element_kernel()
 {
-  return cudaFuncSetAttribute(k_element_mlp, cudaFuncAttributeMaxDynamicSharedMemorySize, el::SMEM);
+  cudaError_t e = cudaFuncSetAttribute(k_element_mlp, cudaFuncAttributeMaxDynamicSharedMemorySize, el::SMEM);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(k_element_mlp, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+  if (e != cudaSuccess) return e;
+  cudaFuncAttributes fa;
+  if ((e = cudaFuncGetAttributes(&fa, k_element_mlp)) != cudaSuccess) return e;
+  int dev = 0, regs_sm = 0, smem_sm = 0, smem_rsv = 0, threads_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev);
+  cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+  cudaDeviceGetAttribute(&smem_rsv, cudaDevAttrReservedSharedMemoryPerBlock, dev);
+  cudaDeviceGetAttribute(&threads_sm, cudaDevAttrMaxThreadsPerMultiProcessor, dev);
+  const int warp_regs = ((fa.numRegs * 32 + 255) / 256) * 256;  // allocated per warp in units of 256
+  const int by_regs   = regs_sm / (warp_regs * 4);
+  const int by_smem   = smem_sm / ((int)fa.sharedSizeBytes + el::SMEM + smem_rsv);
+  const int by_thr    = threads_sm / 128;
+  int       n         = 512 / (int)el::kCols;
+  n                   = by_regs < n ? by_regs : n;
+  n                   = by_smem < n ? by_smem : n;
+  n                   = by_thr < n ? by_thr : n;
+  g_blocks_per_sm     = n < 1 ? 1 : n;
+  return cudaSuccess;
 }
 
 cudaError_t launch_element_mlp(const ElementArgs& a, const MlpElementArgs& m, cudaStream_t stream)
 {
   if (a.E == 0) return cudaSuccess;
-  k_element_mlp<<<(a.E + 127) / 128, 128, el::SMEM, stream>>>(a, m);
+  const long chunks = (a.E + el::kElems - 1) / el::kElems;
+  const long cap    = (long)num_sms() * (g_blocks_per_sm > 0 ? g_blocks_per_sm : 1);
+  const int  grid   = (int)(chunks < cap ? chunks : cap);
+  k_element_mlp<<<grid, 128, el::SMEM, stream>>>(a, m);
   return cudaGetLastError();
 }
 

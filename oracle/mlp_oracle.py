@@ -1,15 +1,15 @@
 """CPU oracle of the learned closure's network (TEST INFRASTRUCTURE ONLY).
 
 The engine's MLP (nimblesm_gb300/csrc/mlp_common.cuh): sigma/G = L(H) +
-s_r * |x|^2 * MLP(x), x = H * s_in, MLP = 9 -> 64 -> 64 -> 6 with GELU, evaluated with BF16
-operands and FP32 accumulation on the tensor cores.  This module restates the
+s_r * |x|^2 * MLP(x), x = H * s_in, MLP = 9 -> 64 -> 64 -> 6 with GELU (tanh
+form), evaluated with BF16 operands and FP32 accumulation on the tensor
+cores.  This module restates the
 forward pass and the gradient of the training loss in float64 numpy, either
 emulating the BF16 roundings at exactly the points where the GPU rounds
 (emulate=True, for a tight gradient check) or in exact arithmetic
 (emulate=False, the mathematical gradient).
 """
 import numpy as np
-from scipy.special import erf
 
 HID, IN, OUT = 64, 9, 6
 oW1, ob1 = 0, HID * IN
@@ -39,12 +39,17 @@ def linear_part(H, k_over_g):
                      H[:, 1] + H[:, 3], H[:, 5] + H[:, 7], H[:, 6] + H[:, 2]], axis=1)
 
 
+GELU_C = np.sqrt(2.0 / np.pi)
+
+
 def gelu(z):
-    return 0.5 * z * (1.0 + erf(z / np.sqrt(2.0)))
+    """GELU, tanh form (the engine's activation)."""
+    return 0.5 * z * (1.0 + np.tanh(GELU_C * (z + 0.044715 * z ** 3)))
 
 
 def gelu_grad(z):
-    return 0.5 * (1.0 + erf(z / np.sqrt(2.0))) + z * np.exp(-0.5 * z * z) / np.sqrt(2.0 * np.pi)
+    t = np.tanh(GELU_C * (z + 0.044715 * z ** 3))
+    return 0.5 * (1.0 + t) + 0.5 * z * (1.0 - t * t) * GELU_C * (1.0 + 3 * 0.044715 * z * z)
 
 
 def forward(P, scales, H, emulate=True):

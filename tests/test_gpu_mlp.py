@@ -99,8 +99,33 @@ def test_fused_element_kernel_matches_predict(mlp):
     m.ComputeInternalForce()
     F, sig = m.GetIntegrationPointData()
     ref, fb = mlp.predict(F.reshape(-1, 9))
-    assert rel(sig.reshape(-1, 6), ref) < 1e-5
+    # predict() sees H = F - I rebuilt from the FP32-stored F: at strains of
+    # ~1e-2 that carries ~6e-8 / 1e-2 relative quantisation in H
+    assert rel(sig.reshape(-1, 6), ref) < 5e-5
     assert m.closure_fallbacks() == fb
+
+
+def test_fused_forces_match_the_material(mlp):
+    """Nodal internal forces of the fused kernel (per-point B^T sigma reduced
+    over each element's lanes, then the deterministic gather) against the
+    plain FP32 element kernel on the same displacement: they differ only by
+    the closure's stress error, on every node."""
+    from nimblesm_gb300.mesh import cube_problem
+    p = cube_problem(8, jitter=0.2, seed=6)
+    rng = np.random.default_rng(8)
+    u = rng.normal(0, 2e-4, size=(p.num_nodes, 3))
+    f = {}
+    for form in ("plain", "mlp"):
+        m = E.Model(p, precision="fp32")
+        if form == "mlp":
+            m.set_closure(mlp)
+        m.SetVectorNodeData("displacement", u)
+        m.ComputeInternalForce()
+        f[form] = m.GetVectorNodeData("internal_force")
+        m.close()
+    assert rel(f["mlp"], f["plain"]) < 2e-3, rel(f["mlp"], f["plain"])
+    scale = np.abs(f["plain"]).max()
+    assert np.abs(f["mlp"] - f["plain"]).max() < 5e-3 * scale
 
 
 def test_small_strain_limit(mlp):

@@ -264,7 +264,6 @@ def mlp_variant(E, args, problem, device, fp64_value, fp32_value):
         res[form] = dict(u=m.GetVectorNodeData("displacement"), sig=sig, drift=(ke + ie - e0) / e0, ms=ms,
                          fallbacks=m.closure_fallbacks(), prof=prof if form == "mlp" else None)
         m.close()
-    mlp.close()
     a, b = res["mlp"], res["fp64"]
     value = 8.0 * problem.num_elem * (steps - 3) / (a["ms"] * 1e-3)
     return {"mlp_closure": {
@@ -276,7 +275,45 @@ def mlp_variant(E, args, problem, device, fp64_value, fp32_value):
         "energy_drift": a["drift"], "energy_drift_fp64": b["drift"], "after_steps": steps,
         "envelope_fallbacks": a["fallbacks"], "training_pairs": args.mlp_pairs, "epochs": args.mlp_epochs,
         "final_loss": loss, "generate_s": t1 - t0, "train_s": t2 - t1,
-        "network": "9-64-64-6 GELU, BF16 weights/activations, FP32 accumulate, tcgen05; linear skip, quadratic gate"}}
+        "network": "9-64-64-6 GELU, BF16 weights/activations, FP32 accumulate, tcgen05; linear skip, quadratic gate"}}, mlp
+
+
+def accuracy_variant(E, args, problem, device, mlp):
+    """The workload's full schedule (2000 steps at dt = 0.5 dt_crit) in the
+    FP64, FP32-mixed and learned-closure forms from the same initial state:
+    each form's displacement and velocity error against the FP64 form after
+    the last step (CUDA graphs of 100 steps; not part of the timed value)."""
+    dt = 0.5 * critical_time_step(problem)
+    steps = args.acc_steps
+    out, ref = {}, None
+    forms = ("fp64", "fp32") + (("mlp",) if mlp is not None else ())
+    for form in forms:
+        m = E.Model(problem, precision="fp64" if form == "fp64" else "fp32", device=device, graph_steps=100)
+        if form == "mlp":
+            m.set_closure(mlp)
+        m.begin(steps * dt, steps, steps)
+        t0 = time.perf_counter()
+        m.advance(1)
+        e0 = sum(m.GetEnergies())
+        m.advance(steps - 1)
+        m.synchronize()
+        wall = time.perf_counter() - t0
+        ke, ie = m.GetEnergies()
+        st = dict(u=m.GetVectorNodeData("displacement"), v=m.GetVectorNodeData("velocity"),
+                  drift=(ke + ie - e0) / e0, wall=wall,
+                  fallbacks=m.closure_fallbacks() if form == "mlp" else 0)
+        m.close()
+        if form == "fp64":
+            ref = st
+            out["fp64"] = {"energy_drift": st["drift"], "wall_s": wall}
+            continue
+        out[form] = {"rel_disp_err_vs_fp64": float(np.linalg.norm(st["u"] - ref["u"]) / np.linalg.norm(ref["u"])),
+                     "rel_vel_err_vs_fp64": float(np.linalg.norm(st["v"] - ref["v"]) / np.linalg.norm(ref["v"])),
+                     "energy_drift": st["drift"], "wall_s": wall}
+        if form == "mlp":
+            out[form]["envelope_fallbacks"] = st["fallbacks"]
+    return {f"accuracy_{steps}_steps": {"steps": steps, "mesh": f"{round(problem.num_elem ** (1 / 3))}^3",
+                                          "forms": out, "bound": 1e-3}}
 
 
 def run_ours(args):
@@ -395,9 +432,15 @@ def run_ours(args):
         variants.update(uq_variants(E, args, local if ws > 1 else 0))
     if args.big_steps > 0:
         variants.update(big_fp32_variant(E, args, local if ws > 1 else 0))
+    mlp = None
     if args.mlp_steps > 0:
         fp32_value = variants.get("fp32", {}).get("value", float("nan"))
-        variants.update(mlp_variant(E, args, problem, local if ws > 1 else 0, value / ws, fp32_value / ws))
+        res, mlp = mlp_variant(E, args, problem, local if ws > 1 else 0, value / ws, fp32_value / ws)
+        variants.update(res)
+    if args.acc_steps > 0:
+        variants.update(accuracy_variant(E, args, problem, local if ws > 1 else 0, mlp))
+    if mlp is not None:
+        mlp.close()
     if variants:
         line["variants"] = variants
     if rank == 0 and not args.no_cpu_baseline:
@@ -426,6 +469,8 @@ def main():
     ap.add_argument("--big-steps", type=int, default=20, help="timed steps of the large variant (0: skip)")
     ap.add_argument("--mlp-steps", type=int, default=103, help="steps of the learned-closure run (0: skip)")
     ap.add_argument("--mlp-pairs", type=int, default=4_000_000)
+    ap.add_argument("--acc-steps", type=int, default=SCHEDULE_STEPS,
+                    help="steps of the FP64 / FP32 / closure accuracy run (0: skip)")
     ap.add_argument("--mlp-epochs", type=int, default=20)
     args = ap.parse_args()
     if args.warmup < 3:

@@ -183,6 +183,26 @@ def ref_cube_fixture(name, n, jitter, seed, steps, output_frequency, sample_elem
     print("wrote", name, r["loop_seconds"], "s", {k: fx[k] for k in fx if str(k).startswith("envelope")})
 
 
+def ref_envelope_fixture(name, n, jitter, seed, steps):
+    """Only the reference's own sensitivity on a long schedule (the state is
+    too large to commit; the tests recompute it with the oracle): the run and
+    the run with the initial velocity perturbed by one ulp (relative 2^-52,
+    seeded signs, as in ref_cube_fixture), compared after the last step."""
+    p = cube_problem(n, jitter=jitter, seed=seed)
+    dt = 0.5 * critical_time_step(p)
+    r = O.run_ref(p, steps * dt, steps, 0)
+    q = cube_problem(n, jitter=jitter, seed=seed)
+    rng = np.random.default_rng(77)
+    q.v_init = q.v_init * (1.0 + rng.choice([-1.0, 1.0], size=q.v_init.shape) * 2.0 ** -52)
+    rq = O.run_ref(q, steps * dt, steps, 0)
+    rel = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))
+    fx = {"n": n, "jitter": jitter, "seed": seed, "steps": steps, "dt_crit": r["dt_crit"],
+          "envelope_u": rel(rq["u"], r["u"]), "envelope_v": rel(rq["v"], r["v"]),
+          "envelope_sigma": rel(rq["sigma"], r["sigma"])}
+    np.savez_compressed(os.path.join(HERE, f"ref_{name}.npz"), **fx)
+    print("wrote", name, {k: fx[k] for k in fx if str(k).startswith("envelope")})
+
+
 def ref_points_fixture():
     """Stress and single-element known answers from the reference."""
     rng = np.random.default_rng(2024)
@@ -255,3 +275,4 @@ if __name__ == "__main__":
     ref_cube_fixture("cube4_jitter", 4, 0.2, 7, 20, 0)
     ref_cube_fixture("cube16_cfg0", 16, 0.0, 0, 500, 500, sample_elems=64)
     ref_gold_rerun()
+    ref_envelope_fixture("cube40_schedule", 40, 0.2, 0, 2000)

@@ -26,13 +26,18 @@ def _built():
     O.build(ref=False)
 
 
-def compare(gpu, ref, keys=("u", "v", "sigma"), tol=TOL, sigma_tol=None):
-    """u, v within 1e-10 of the reference.  sigma within 1e-10 or, where the
-    reference itself is less reproducible than that, within twice its measured
-    sensitivity (sigma_tol, from the reference: a 1-ulp input perturbation or
-    its stress-evaluation error against extended precision)."""
+def compare(gpu, ref, keys=("u", "v", "sigma"), tol=TOL, sigma_tol=None, v_tol=None):
+    """u, v within 1e-10 of the reference.  sigma (and, on long schedules, v)
+    within 1e-10 or, where the reference itself is less reproducible than
+    that, within twice its measured sensitivity (sigma_tol / v_tol, from the
+    reference: a 1-ulp input perturbation or its stress-evaluation error
+    against extended precision)."""
     for k in keys:
-        t = max(tol, sigma_tol) if (k == "sigma" and sigma_tol) else tol
+        t = tol
+        if k == "sigma" and sigma_tol:
+            t = max(tol, sigma_tol)
+        if k == "v" and v_tol:
+            t = max(tol, v_tol)
         e = rel(gpu[k], ref[k])
         assert e <= t, f"{k}: relative error {e:.3e} > {t:.3e}"
 
@@ -242,4 +247,31 @@ def test_128_cube_first_steps_against_oracle():
     # the engine's stress is itself accurate: within 1e-10 of the
     # extended-precision stress of its own displacement
     assert rel(g["sigma"][idx], O.stress_exact(p, g["u"], idx)) < TOL
+    m.close()
+
+
+def test_full_schedule_against_oracle():
+    """The workload's whole schedule, 2000 steps at dt = 0.5 dt_crit, on a
+    40^3 jittered cube (the 128^3 benchmark mesh's construction, 512k
+    integration points): FP64 parity with the oracle after the last step.
+    Over 2000 steps the reference's own velocity and stress move by
+    1.7e-10 / 1.1e-10 under a 1-ulp perturbation of the initial velocity
+    (ref_cube40_schedule, measured on the reference), so v and sigma are held
+    to twice that; u to 1e-10."""
+    import os
+    fx = load("ref_cube40_schedule")
+    p = cube_problem(40, jitter=0.2, seed=0)
+    dt = 0.5 * critical_time_step(p)
+    steps = 2000
+    run = O.PortRun(p, threads=os.cpu_count())
+    run.begin(steps * dt, steps, 0)
+    run.advance(steps)
+    ref = run.state()
+    assert run.dt_crit == float(fx["dt_crit"])
+    m = E.Model(p, graph_steps=100)
+    m.begin(steps * dt, steps, 0)
+    m.advance(steps)
+    g = m.state()
+    floor, idx = sigma_floor(p, ref)
+    compare(g, ref, sigma_tol=max(floor, 2.0 * float(fx["envelope_sigma"])), v_tol=2.0 * float(fx["envelope_v"]))
     m.close()

@@ -277,6 +277,13 @@ int nsm_closure_fallbacks(nsm_model* model, unsigned long long* count);
  * N, K multiples of 16, N <= 256, K <= 128; host arrays. */
 int nsm_tc_selftest(int N, int K, const float* A, const float* B, float* D);
 
+/* Diagnostic of the failure path of the tensor-core waits: a kernel that
+ * holds tensor memory waits on an mbarrier phase that nothing completes,
+ * bounded by `polls` (1..100000) polls; *timed_out = 1 when the wait ran
+ * out, after which the kernel freed its tensor memory and returned.  The
+ * context stays usable. */
+int nsm_tc_wait_timeout_selftest(long polls, int* timed_out);
+
 /* Pinned host memory for the host-buffer entry points (page-locked so that the
  * copies run at full link bandwidth). */
 void* nsm_host_alloc(size_t bytes);

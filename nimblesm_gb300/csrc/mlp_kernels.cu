@@ -354,7 +354,10 @@ __global__ void __launch_bounds__(128) k_train(const float* __restrict__ X, cons
   if (r == 0) loss_partial[blockIdx.x] = red[0];
 
 cleanup:
-  if (r == 0 && err) atomicOr(status, NSM_STATUS_TIMEOUT);
+  if (r == 0 && err) {
+    mbar_wait(sy.mbar, sy.phase ^ 1u);  // bounded: let a timed-out MMA drain before the columns are freed
+    atomicOr(status, NSM_STATUS_TIMEOUT);
+  }
   fence_before_sync();
   __syncthreads();
   if (warp == 0) tmem_dealloc(tb, tr::kCols);
@@ -488,7 +491,10 @@ __global__ void __launch_bounds__(128) k_predict(long n, const float* __restrict
     }
   }
 cleanup:
-  if (r == 0 && err) atomicOr(status, NSM_STATUS_TIMEOUT);
+  if (r == 0 && err) {
+    mbar_wait(sy.mbar, sy.phase ^ 1u);  // bounded: let a timed-out MMA drain before the columns are freed
+    atomicOr(status, NSM_STATUS_TIMEOUT);
+  }
   fence_before_sync();
   __syncthreads();
   if (warp == 0) tmem_dealloc(tslot, inf::kCols);

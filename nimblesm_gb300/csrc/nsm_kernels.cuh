@@ -8,7 +8,6 @@
 // Device status word bits (read back by the host, returned as C status codes).
 #define NSM_STATUS_BAD_JACOBIAN 1   // a non-positive Jacobian determinant (inverted element)
 #define NSM_STATUS_NONFINITE 2      // a NaN or Inf in a stress or force
-#define NSM_STATUS_MLP_FALLBACK 4   // points left the learned closure's envelope (informational)
 #define NSM_STATUS_TIMEOUT 8        // a bounded wait on the tensor cores ran out
 
 namespace nsm {

@@ -144,6 +144,7 @@ int read_status(nsm_model* m)
   NSM_CUDA(cudaStreamSynchronize(m->stream));
   if (status & NSM_STATUS_BAD_JACOBIAN) return fail(NSM_ERR_BAD_JACOBIAN, "non-positive Jacobian (inverted element)");
   if (status & NSM_STATUS_NONFINITE) return fail(NSM_ERR_NONFINITE, "non-finite element force");
+  if (status & NSM_STATUS_TIMEOUT) return fail(NSM_ERR_STATE, "a bounded tensor-core wait ran out (learned closure)");
   return NSM_OK;
 }
 

@@ -69,7 +69,47 @@ __global__ void __launch_bounds__(128) k_tc_selftest(int N, int K, const float* 
   if (warp == 0) tmem_dealloc(tbase, ncols);
 }
 
+// The failure path of every tensor-core wait: tensor memory held, a wait on
+// an mbarrier phase that nothing completes, bounded by `polls`; the kernel
+// records the timeout, frees its columns and returns.
+__global__ void __launch_bounds__(128) k_tc_wait_timeout(long polls, int* __restrict__ status)
+{
+  __shared__ uint64_t mbar;
+  __shared__ uint32_t tmem_slot;
+  const int           tid = threadIdx.x, warp = tid >> 5;
+  if (warp == 0) {
+    tmem_alloc(&tmem_slot, 32);
+    tmem_relinquish();
+  }
+  if (tid == 0) mbar_init(&mbar, 1);
+  fence_before_sync();
+  __syncthreads();
+  fence_after_sync();
+  const bool done = mbar_wait(&mbar, 0, polls);  // no arrival is ever made
+  if (!done && tid == 0) atomicOr(status, 1);
+  fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tmem_dealloc(tmem_slot, 32);
+}
+
 }  // namespace
+
+extern "C" int nsm_tc_wait_timeout_selftest(long polls, int* timed_out)
+{
+  if (!timed_out || polls < 1 || polls > 100000) return NSM_ERR_INVALID_ARGUMENT;
+  int* dS = nullptr;
+  int  rc = NSM_OK, status = 0;
+  if (cudaMalloc(&dS, sizeof(int)) != cudaSuccess || cudaMemset(dS, 0, sizeof(int)) != cudaSuccess) rc = NSM_ERR_CUDA;
+  if (rc == NSM_OK) {
+    k_tc_wait_timeout<<<1, 128>>>(polls, dS);
+    if (cudaDeviceSynchronize() != cudaSuccess ||
+        cudaMemcpy(&status, dS, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+      rc = NSM_ERR_CUDA;
+  }
+  cudaFree(dS);
+  *timed_out = status;
+  return rc;
+}
 
 extern "C" int nsm_tc_selftest(int N, int K, const float* A, const float* B, float* D)
 {

@@ -102,6 +102,7 @@ SIGNATURES = {
     "nsm_set_mlp_closure": (C.c_int, [_vp, _vp]),
     "nsm_closure_fallbacks": (C.c_int, [_vp, C.POINTER(C.c_ulonglong)]),
     "nsm_tc_selftest": (C.c_int, [C.c_int, C.c_int, _dp_f, _dp_f, _dp_f]),
+    "nsm_tc_wait_timeout_selftest": (C.c_int, [C.c_long, C.POINTER(C.c_int)]),
     "nsm_host_alloc": (_vp, [C.c_size_t]),
     "nsm_host_free": (None, [_vp]),
 }

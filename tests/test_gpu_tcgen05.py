@@ -32,3 +32,15 @@ def test_tcgen05_gemm(N, K):
     ref = bf16(A).astype(np.float64) @ bf16(Bm).astype(np.float64).T
     err = np.abs(D - ref).max() / np.abs(ref).max()
     assert err < 1e-5, err
+
+
+def test_bounded_wait_times_out_and_context_stays_usable():
+    """Every tensor-core wait is bounded: a wait that nothing completes runs
+    out, the kernel frees its tensor memory and reports, and the next
+    tensor-core kernel in the same context runs normally."""
+    from nimblesm_gb300 import build as B
+    B.build()
+    flag = C.c_int(0)
+    assert E.library().nsm_tc_wait_timeout_selftest(1000, C.byref(flag)) == 0
+    assert flag.value == 1
+    test_tcgen05_gemm(64, 32)

@@ -154,6 +154,15 @@ int nsm_compute_internal_force_host(nsm_model* model, const double* displacement
  * F: [E][8][9], sigma: [E][8][6]; either may be NULL. */
 int nsm_get_ip_data(nsm_model* model, double* F, double* sigma);
 
+/* Derived element output of the current configuration (replaces
+ * Block::ComputeDerivedElementData, src/nimble_block.cc:438-497, through
+ * HexElement::ComputeVolumeAverage, src/nimble_element.cc:262-282): element
+ * volume [E] and volume-averaged stress [E][6] (weights det J of the current
+ * configuration X + u), from the point stresses of the last evaluation that
+ * stored point data.  Same operations in the same order as the reference.
+ * Either output may be NULL. */
+int nsm_compute_derived_element_data(nsm_model* model, double* volume, double* stress);
+
 /* Kinetic energy 1/2 sum m v.v and internal energy sum det(J_X) W(F) over the
  * integration points (not in the reference; used for energy balance). */
 int nsm_get_energies(nsm_model* model, double* kinetic, double* internal);

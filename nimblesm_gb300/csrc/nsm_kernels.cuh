@@ -41,6 +41,11 @@ struct SetupArgs {
 void        shape_tables(double* N, double* dN);
 cudaError_t upload_shape_tables(cudaStream_t stream);
 cudaError_t launch_setup(const SetupArgs& a, cudaStream_t stream);
+// Element volume [E] and volume-averaged stress [E][6] of the current
+// configuration from the point records (setup_kernels.cu).
+cudaError_t launch_derived_element(int E, long ld_e, const int* conn, const double* X, const double* u, long ld_n,
+                                   const void* ip, int ip_is_float, double* volume, double* avg, int* status,
+                                   cudaStream_t stream);
 
 // Per-point record of the element data: 16 values of type T per element and
 // integration point, records laid out [ip][ld_e][16]: slots 0..8 F in the

@@ -746,6 +746,26 @@ int nsm_get_ip_data(nsm_model* m, double* F, double* sigma)
   return NSM_OK;
 }
 
+int nsm_compute_derived_element_data(nsm_model* m, double* volume, double* stress)
+{
+  if (!m) return fail(NSM_ERR_INVALID_ARGUMENT, "null model");
+  NSM_CUDA(cudaSetDevice(m->device));
+  if (m->E == 0) return NSM_OK;
+  const int is_float = m->precision == NSM_PRECISION_FP64 ? 0 : 1;
+  double*   tmp      = nullptr;
+  NSM_CUDA(cudaMalloc(&tmp, sizeof(double) * 7 * (size_t)m->E));
+  cudaError_t e = nsm::launch_derived_element(m->E, m->ld_e, m->d_conn, m->d_X, m->d_u, m->ld_n, m->d_ip, is_float,
+                                              tmp, tmp + m->E, m->d_status, m->stream);
+  if (e == cudaSuccess && volume)
+    e = cudaMemcpyAsync(volume, tmp, sizeof(double) * (size_t)m->E, cudaMemcpyDeviceToHost, m->stream);
+  if (e == cudaSuccess && stress)
+    e = cudaMemcpyAsync(stress, tmp + m->E, sizeof(double) * 6 * (size_t)m->E, cudaMemcpyDeviceToHost, m->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(m->stream);
+  cudaFree(tmp);
+  if (e != cudaSuccess) return cuda_fail(e, "nsm_compute_derived_element_data");
+  return read_status(m);
+}
+
 int nsm_get_energies(nsm_model* m, double* kinetic, double* internal)
 {
   if (!m) return fail(NSM_ERR_INVALID_ARGUMENT, "null model");

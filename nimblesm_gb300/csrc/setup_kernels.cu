@@ -192,6 +192,75 @@ __global__ void k_min_reduce(long n, const double* __restrict__ in, double* __re
   if (threadIdx.x == 0) out[blockIdx.x] = s[0];
 }
 
+// Derived element output (Block::ComputeDerivedElementData,
+// src/nimble_block.cc:438-497 -> HexElement::ComputeVolumeAverage,
+// src/nimble_element.cc:262-282 and src/nimble_element.h:343-392): the
+// current coordinates x = X + u, at each point the current Jacobian
+// sum_n (x_n + 0) (x) dN_n/dxi and its determinant (Invert3x3), the element
+// volume sum_p det_p and the volume-averaged stress sum_p (sigma_p w_p) det_p
+// / volume, w_p = 1.  The operations and their order are the reference's and
+// this file is compiled without FMA contraction, so for the same u and
+// point stresses the result is the reference's bit for bit.
+template <typename TR>
+__global__ void k_derived_element(int E, long ld_e, const int* __restrict__ conn, const double* __restrict__ X,
+                                  const double* __restrict__ u, long ld_n, const TR* __restrict__ ip,
+                                  double* __restrict__ volume, double* __restrict__ avg, int* __restrict__ status)
+{
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= E) return;
+  double x[8][3];
+#pragma unroll
+  for (int n = 0; n < 8; n++) {
+    int id = conn[n * ld_e + e];
+#pragma unroll
+    for (int k = 0; k < 3; k++) x[n][k] = X[k * ld_n + id] + u[k * ld_n + id];
+  }
+  double vol = 0.0, acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  bool   bad = false;
+#pragma unroll 1
+  for (int p = 0; p < 8; p++) {
+    double a[3][3] = {{0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}};
+    for (int j = 0; j < 8; j++) {
+      const double* d  = &c_dN[24 * p + 3 * j];
+      const double  c0 = x[j][0] + 0.0, c1 = x[j][1] + 0.0, c2 = x[j][2] + 0.0;
+      a[0][0] += c0 * d[0];
+      a[0][1] += c0 * d[1];
+      a[0][2] += c0 * d[2];
+      a[1][0] += c1 * d[0];
+      a[1][1] += c1 * d[1];
+      a[1][2] += c1 * d[2];
+      a[2][0] += c2 * d[0];
+      a[2][1] += c2 * d[1];
+      a[2][2] += c2 * d[2];
+    }
+    double    ai[3][3];
+    const double det = invert3x3(a, ai);
+    if (!(det > 0.0)) bad = true;
+    vol += det;
+    const TR* rec = ip + ((size_t)p * ld_e + e) * kIpRecord;
+#pragma unroll
+    for (int q = 0; q < 6; q++) acc[q] += (double)rec[9 + q] * 1.0 * det;
+  }
+#pragma unroll
+  for (int q = 0; q < 6; q++) avg[6 * (size_t)e + q] = acc[q] / vol;
+  volume[e] = vol;
+  if (bad) atomicOr(status, NSM_STATUS_BAD_JACOBIAN);
+}
+
+cudaError_t launch_derived_element(int E, long ld_e, const int* conn, const double* X, const double* u, long ld_n,
+                                   const void* ip, int ip_is_float, double* volume, double* avg, int* status,
+                                   cudaStream_t stream)
+{
+  if (E == 0) return cudaSuccess;
+  if (ip_is_float)
+    k_derived_element<float><<<grid_for(E, 128), 128, 0, stream>>>(E, ld_e, conn, X, u, ld_n, (const float*)ip, volume,
+                                                                   avg, status);
+  else
+    k_derived_element<double><<<grid_for(E, 128), 128, 0, stream>>>(E, ld_e, conn, X, u, ld_n, (const double*)ip,
+                                                                     volume, avg, status);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_setup(const SetupArgs& a, cudaStream_t stream)
 {
   k_setup_elements<<<grid_for(a.E, 128), 128, 0, stream>>>(a.E, a.ld_e, a.conn, a.X, a.ld_n, a.elem_group, a.mats,

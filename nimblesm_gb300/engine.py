@@ -69,6 +69,7 @@ SIGNATURES = {
     "nsm_compute_internal_force": (C.c_int, [_vp, C.c_double, C.c_double, C.c_int]),
     "nsm_compute_internal_force_host": (C.c_int, [_vp, _dp, _dp]),
     "nsm_get_ip_data": (C.c_int, [_vp, _dp, _dp]),
+    "nsm_compute_derived_element_data": (C.c_int, [_vp, _dp, _dp]),
     "nsm_get_energies": (C.c_int, [_vp, _dp, _dp]),
     "nsm_begin": (C.c_int, [_vp, C.c_double, C.c_double, C.c_int, C.c_int, _dp]),
     "nsm_advance": (C.c_int, [_vp, C.c_int]),
@@ -240,6 +241,14 @@ class Model:
         F, s = np.zeros((E, 8, 9)), np.zeros((E, 8, 6))
         _check(library().nsm_get_ip_data(self._h, _d(F), _d(s)))
         return F, s
+
+    def ComputeDerivedElementData(self):
+        """Element volume [E] and volume-averaged stress [E][6] of the current
+        configuration (Block::ComputeDerivedElementData)."""
+        E = self.problem.num_elem
+        vol, s = np.zeros(E), np.zeros((E, 6))
+        _check(library().nsm_compute_derived_element_data(self._h, _d(vol), _d(s)))
+        return vol, s
 
     def GetEnergies(self):
         ke, ie = C.c_double(), C.c_double()

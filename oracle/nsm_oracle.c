@@ -424,6 +424,47 @@ gather_element(const nsm_oracle_model* m, int e, const double* field, double* ou
   }
 }
 
+/* HexElement::ComputeVolumeAverage (src/nimble_element.cc:262-282) ->
+ * ComputeVolumeAverageQuantities_impl (src/nimble_element.h:343-392) for the
+ * 6 stress components: the element's coordinates enter as "reference"
+ * coordinates plus a zero displacement, the current Jacobian and its
+ * determinant come from Invert3x3 at each point, volume = sum det, and the
+ * average sums q * w * det with w = 1 before one division by the volume. */
+void
+nsm_oracle_volume_average(const double* x, const double* q, double* volume, double* avg)
+{
+  build_tables();
+  double cc[24];
+  for (int i = 0; i < 24; i++) cc[i] = x[i] + 0.0;
+  double vol = 0.0, acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  for (int ip = 0; ip < 8; ip++) {
+    double a[3][3], a_inv[3][3];
+    jacobian(cc, ip, a);
+    double det = invert3x3(a, a_inv);
+    vol += det;
+    for (int k = 0; k < 6; k++) acc[k] += q[6 * ip + k] * 1.0 * det;
+  }
+  for (int k = 0; k < 6; k++) avg[k] = acc[k] / vol;
+  *volume = vol;
+}
+
+/* Block::ComputeDerivedElementData (src/nimble_block.cc:438-497): current
+ * coordinates X + u per element (:477-483), then the volume average of the
+ * element's point stresses. */
+void
+nsm_oracle_derived_element_data(const nsm_oracle_model* m, const double* u, const double* sigma, double* volume,
+                                double* avg)
+{
+  for (int e = 0; e < m->num_elem; e++) {
+    double x[24];
+    for (int n = 0; n < 8; n++) {
+      int id = m->conn[8 * e + n];
+      for (int k = 0; k < 3; k++) x[3 * n + k] = m->coords[3 * id + k] + u[3 * id + k];
+    }
+    nsm_oracle_volume_average(x, sigma + 48 * (size_t)e, volume + e, avg + 6 * (size_t)e);
+  }
+}
+
 /* Lumped mass of one element: row sums of the consistent mass
  * (src/nimble_element.h:266-309, src/nimble_element.cc:173-193). */
 static void

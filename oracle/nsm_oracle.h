@@ -72,11 +72,21 @@ void nsm_oracle_nodal_forces(const double* x, const double* sigma, double* f);
 void nsm_oracle_element(
     const double* X, const double* u, double bulk_modulus, double shear_modulus, double* F, double* sigma, double* f);
 
+/* Volume average of one element's point stresses (src/nimble_element.cc:262-282,
+ * src/nimble_element.h:343-392): x [8][3] current coordinates, q [8][6];
+ * volume and avg [6] out. */
+void nsm_oracle_volume_average(const double* x, const double* q, double* volume, double* avg);
+
 /* Lumped mass (src/nimble_model_data.cc:495-530, src/nimble_block.cc:110-146,
  * src/nimble_element.cc:173-193) and critical time step
  * (src/nimble_block_base.cc:51-84, src/nimble_element.cc:221-260). */
 void   nsm_oracle_lumped_mass(const nsm_oracle_model* m, double* mass);
 double nsm_oracle_critical_time_step(const nsm_oracle_model* m);
+
+/* Derived element output over a model (src/nimble_block.cc:438-497): u [N][3],
+ * sigma [E][8][6] -> volume [E], avg [E][6]. */
+void nsm_oracle_derived_element_data(const nsm_oracle_model* m, const double* u, const double* sigma, double* volume,
+                                     double* avg);
 
 /* Strain energy density W(F) whose Cauchy stress is the reference's
  * neo-Hookean stress: W = K/4 (J^2-1) - K/2 ln J + G/2 (J^{-2/3} tr(F F^T) - 3).

@@ -96,6 +96,8 @@ def port():
         lib.nsm_oracle_set_state.argtypes = [C.c_void_p, _dp, _dp, _dp]
         lib.nsm_oracle_energies.argtypes = [C.c_void_p, _dp, _dp]
         lib.nsm_oracle_stress_exact.argtypes = [C.POINTER(_Model), _dp, C.c_int, _ip, _dp]
+        lib.nsm_oracle_volume_average.argtypes = [_dp, _dp, _dp, _dp]
+        lib.nsm_oracle_derived_element_data.argtypes = [C.POINTER(_Model), _dp, _dp, _dp, _dp]
         _port = lib
     return _port
 
@@ -115,6 +117,7 @@ def ref():
                                    _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp]
         lib.nimref_element.argtypes = [_dp, _dp, C.c_double, C.c_double, C.c_double, _dp, _dp, _dp]
         lib.nimref_stress.argtypes = [C.c_int, _dp, C.c_double, C.c_double, _dp]
+        lib.nimref_volume_average.argtypes = [_dp, _dp, _dp, _dp]
         lib.nimref_last_error.restype = C.c_char_p
         _ref = lib
     return _ref
@@ -278,6 +281,32 @@ def stress_exact(problem, u, elems):
     out = np.zeros((len(elems), 8, 6))
     port().nsm_oracle_stress_exact(C.byref(m), _d(u), len(elems), _i(elems), _d(out))
     return out
+
+
+def volume_average(x_cur, sigma, which="port"):
+    """One element's volume and volume-averaged stress (x_cur [8,3], sigma
+    [8,6]) -> (volume, avg [6]), HexElement::ComputeVolumeAverage."""
+    x = np.ascontiguousarray(x_cur, dtype=np.float64)
+    q = np.ascontiguousarray(sigma, dtype=np.float64)
+    vol, avg = C.c_double(0.0), np.zeros(6)
+    if which == "port":
+        port().nsm_oracle_volume_average(_d(x), _d(q), C.cast(C.pointer(vol), _dp), _d(avg))
+    else:
+        if ref().nimref_volume_average(_d(x), _d(q), C.cast(C.pointer(vol), _dp), _d(avg)) != 0:
+            raise RuntimeError(ref().nimref_last_error().decode())
+    return vol.value, avg
+
+
+def derived_element_data(problem, u, sigma):
+    """Element volume [E] and volume-averaged stress [E,6] of displacement u
+    ([N,3]) and point stresses sigma ([E,8,6]), Block::ComputeDerivedElementData."""
+    keep = []
+    m = _model(problem, keep)
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    q = np.ascontiguousarray(sigma, dtype=np.float64)
+    vol, avg = np.zeros(problem.num_elem), np.zeros((problem.num_elem, 6))
+    port().nsm_oracle_derived_element_data(C.byref(m), _d(u), _d(q), _d(vol), _d(avg))
+    return vol, avg
 
 
 def shape_tables():

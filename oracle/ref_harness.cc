@@ -356,4 +356,20 @@ nimref_stress(int n, const double* F, double bulk_modulus, double shear_modulus,
   }
 }
 
+/* The reference's volume average of one element's point stresses,
+ * HexElement::ComputeVolumeAverage (src/nimble_element.cc:262-282):
+ * x_cur [8][3], sigma [8][6] -> volume, avg [6]. */
+int
+nimref_volume_average(const double* x_cur, const double* sigma, double* volume, double* avg)
+{
+  try {
+    nimble::HexElement element;
+    element.ComputeVolumeAverage(x_cur, 6, sigma, *volume, avg);
+    return 0;
+  } catch (std::exception const& ex) {
+    g_last_error = ex.what();
+    return -1;
+  }
+}
+
 }  // extern "C"

@@ -203,6 +203,23 @@ def ref_envelope_fixture(name, n, jitter, seed, steps):
     print("wrote", name, {k: fx[k] for k in fx if str(k).startswith("envelope")})
 
 
+def ref_derived_fixture(name="cube4_jitter"):
+    """Derived element output of the reference (element volume and
+    volume-averaged stress, HexElement::ComputeVolumeAverage through
+    nimref_volume_average) on the final state of the ref_<name> fixture, with
+    the current coordinates formed as Block::ComputeDerivedElementData forms
+    them (reference coordinates + displacement, src/nimble_block.cc:477-483)."""
+    fx = np.load(os.path.join(HERE, f"ref_{name}.npz"))
+    p = cube_problem(int(fx["n"]), jitter=float(fx["jitter"]), seed=int(fx["seed"]))
+    vol, avg = np.zeros(p.num_elem), np.zeros((p.num_elem, 6))
+    for e in range(p.num_elem):
+        ids = p.conn[e]
+        x = p.coords[ids] + fx["u"][ids]
+        vol[e], avg[e] = O.volume_average(x, fx["sigma"][e], which="ref")
+    np.savez_compressed(os.path.join(HERE, f"ref_derived_{name}.npz"), volume=vol, stress=avg)
+    print("wrote derived", name)
+
+
 def ref_points_fixture():
     """Stress and single-element known answers from the reference."""
     rng = np.random.default_rng(2024)
@@ -276,3 +293,4 @@ if __name__ == "__main__":
     ref_cube_fixture("cube16_cfg0", 16, 0.0, 0, 500, 500, sample_elems=64)
     ref_gold_rerun()
     ref_envelope_fixture("cube40_schedule", 40, 0.2, 0, 2000)
+    ref_derived_fixture("cube4_jitter")

@@ -275,3 +275,34 @@ def test_full_schedule_against_oracle():
     floor, idx = sigma_floor(p, ref)
     compare(g, ref, sigma_tol=max(floor, 2.0 * float(fx["envelope_sigma"])), v_tol=2.0 * float(fx["envelope_v"]))
     m.close()
+
+
+def test_derived_element_data():
+    """Derived element output (element volume and volume-averaged stress,
+    Block::ComputeDerivedElementData): bitwise the oracle's restatement
+    applied to the engine's own displacement and point stresses (same
+    operations in the same order, no FMA contraction), and within the stress
+    tolerance of the oracle run's derived output.  The FP32-mixed form's
+    derived output is within 1e-3 of the FP64 form's."""
+    p = cube_problem(8, jitter=0.2, seed=3)
+    dt = 0.5 * critical_time_step(p)
+    steps = 60
+    ref = O.run_port(p, steps * dt, steps, 0)
+    m = E.Model(p)
+    m.begin(steps * dt, steps, 0)
+    m.advance(steps)
+    g = m.state()
+    vol, avg = m.ComputeDerivedElementData()
+    v_own, a_own = O.derived_element_data(p, g["u"], g["sigma"])
+    assert np.array_equal(vol, v_own) and np.array_equal(avg, a_own)
+    v_ref, a_ref = O.derived_element_data(p, ref["u"], ref["sigma"])
+    floor, _ = sigma_floor(p, ref)
+    assert rel(vol, v_ref) < TOL
+    assert rel(avg, a_ref) < max(TOL, floor)
+    m.close()
+    m32 = E.Model(p, precision="fp32")
+    m32.begin(steps * dt, steps, 0)
+    m32.advance(steps)
+    v32, a32 = m32.ComputeDerivedElementData()
+    assert rel(v32, vol) < 1e-6 and rel(a32, avg) < 1e-3
+    m32.close()

@@ -45,6 +45,19 @@ def test_cube_runs_match_reference_bitwise(name):
         assert np.linalg.norm(r["sigma"]) == float(fx["sigma_norm"])
 
 
+def test_derived_element_data_matches_reference_bitwise():
+    """Element volume and volume-averaged stress (Block::ComputeDerivedElementData)
+    on the reference's final state of the 4^3 run, against the reference's own
+    HexElement::ComputeVolumeAverage."""
+    fx = load("ref_cube4_jitter")
+    dx = load("ref_derived_cube4_jitter")
+    p = cube_problem(int(fx["n"]), jitter=float(fx["jitter"]), seed=int(fx["seed"]))
+    vol, avg = O.derived_element_data(p, fx["u"], fx["sigma"])
+    assert np.array_equal(vol, dx["volume"])
+    assert np.array_equal(avg, dx["stress"])
+    assert abs(vol.sum() - 1.0) < 1e-3  # the unit cube, slightly deformed
+
+
 def test_numpy_critical_time_step_matches_oracle():
     p = cube_problem(6, jitter=0.2, seed=11)
     keep = []

@@ -39,6 +39,10 @@ FALLBACK_HBM_GBS = 6800.0
 METRIC = "hex8 IP stress updates/sec, plain FP64 vs mixed/MLP at <=1e-3 rel. disp error"
 UNIT = "IP-updates/s"
 SCHEDULE_STEPS = 2000  # the workload's schedule: dt = 0.5 dt_crit, 2000 steps
+# FP64 flops per integration point of the FP64 element kernel's formulation:
+# 122.0 DFMA (2 flops each) + 31.5 DADD + 65.1 DMUL executed per point
+# (ncu on the 64^3 case, profiles/k_element_fp64_cube64.md).
+FP64_FLOPS_PER_IP = 340.6
 
 
 def algorithmic_bytes(N, E, precision):
@@ -113,9 +117,11 @@ def dist_env():
     return ws, rank, local
 
 
-def cpu_baseline(problem, dt, seconds_budget=15.0, threads=None):
-    """The oracle (C restatement of the reference's host path) on all host
-    cores, from the workload's initial state, on a bounded number of steps."""
+def cpu_baseline(problem, dt, seconds_budget=15.0, threads=None, max_steps=40):
+    """The oracle (C restatement of the reference's host path, whose gather
+    assembly is the reference's serial order at any thread count) on all host
+    cores, or on the given number of threads, from the workload's initial
+    state, on a bounded number of steps."""
     from oracle import oracle
 
     oracle.build(ref=False)
@@ -125,7 +131,7 @@ def cpu_baseline(problem, dt, seconds_budget=15.0, threads=None):
     v[problem.node_sets["nodelist_1"]] = 0.0
     a = np.zeros_like(u)
     t1 = oracle.continue_port(problem, u, v, a, 0.0, dt, 1, threads)  # includes first-touch
-    k = int(max(1, min(40, seconds_budget / max(t1, 1e-3))))
+    k = int(max(1, min(max_steps, seconds_budget / max(t1, 1e-3))))
     secs = oracle.continue_port(problem, u, v, a, dt, dt, k, threads)
     return {"value": 8.0 * problem.num_elem * k / secs, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"{k} steps of the same {round(problem.num_elem ** (1 / 3))}^3 mesh from its initial state "
@@ -418,6 +424,18 @@ def run_ours(args):
                      "step_algorithmic_bytes": step_bytes},
         "clocks": head["clocks"],
     }
+    if args.precision == "fp64":
+        # the roof that binds the FP64 element kernel: the FP64 pipe
+        peak64 = E.fp64_peak_tflops(local if ws > 1 else 0)
+        ach64 = FP64_FLOPS_PER_IP * 8 * E_ / (elem_ms * 1e-3) / 1e12
+        sms = E.device_sm_count(local if ws > 1 else 0)
+        max_mhz = (head["clocks"] or {}).get("sm_max_mhz") or 2070.0
+        nominal = 2 * 2 * sms * max_mhz * 1e6 / 1e12  # 2 DFMA (4 flops) per SM per cycle at the maximum clock
+        line["roofline_fp64"] = {"bound": "fp64", "kernel": "k_element", "achieved": ach64, "peak": peak64,
+                                 "unit": "TFLOP/s", "frac": ach64 / peak64, "peak_source": "measured (DFMA probe)",
+                                 "peak_nominal": nominal, "frac_nominal": ach64 / nominal,
+                                 "flops_per_ip": FP64_FLOPS_PER_IP,
+                                 "flops_source": "executed DFMA/DADD/DMUL per point, ncu (FMA = 2 flops)"}
     variants = {}
     for prec, r in results.items():
         if prec == args.precision:
@@ -445,6 +463,7 @@ def run_ours(args):
         line["variants"] = variants
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(problem, dt)
+        line["cpu_baseline"]["single_core"] = cpu_baseline(problem, dt, seconds_budget=8.0, threads=1, max_steps=4)
     m.close()
     if rank == 0:
         print(json.dumps(line), flush=True)

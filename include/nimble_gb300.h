@@ -79,6 +79,19 @@ typedef struct nsm_neohookean {
   double shear_modulus;
 } nsm_neohookean;
 
+/* A material of any supported model: the reference's material line
+ * "<model> density .. bulk_modulus .. shear_modulus .." as MaterialFactory
+ * creates it (src/nimble_material_factory.cc:57-70). */
+#define NSM_MATERIAL_NEOHOOKEAN 0 /* NeohookeanMaterial, src/nimble_material.cc:208-310 */
+#define NSM_MATERIAL_ELASTIC 1    /* ElasticMaterial (small strain on the unrotated F), src/nimble_material.cc:59-126 */
+typedef struct nsm_material {
+  int    model; /* NSM_MATERIAL_* */
+  int    reserved;
+  double density;
+  double bulk_modulus;
+  double shear_modulus;
+} nsm_material;
+
 typedef struct nsm_options {
   int precision;     /* NSM_PRECISION_* */
   int store_ip_data; /* 1: write F and sigma per integration point every step (the
@@ -109,6 +122,16 @@ int nsm_destroy(nsm_model* model);
  * shares one mesh).  meshes, materials: [num_samples]. */
 int nsm_create_ensemble(int num_samples, const nsm_mesh_desc* meshes, const nsm_neohookean* materials,
                         const nsm_options* options, nsm_model** out);
+
+/* One mesh of several element blocks, each with its own material of any model
+ * (ModelData::InitializeBlocks over all blocks, src/nimble_model_data.cc:484-493,
+ * one Block and Material per "element block" line).  elem_block [E]: block
+ * index 0..num_blocks-1 of each element, non-decreasing (the elements of a
+ * block are contiguous, in the reference's block-by-block order, which is
+ * also its assembly order); materials [num_blocks].  num_blocks = 1 with
+ * elem_block NULL is a single block of any material model. */
+int nsm_create_blocks(const nsm_mesh_desc* mesh, int num_blocks, const int* elem_block, const nsm_material* materials,
+                      const nsm_options* options, nsm_model** out);
 int nsm_ensemble_offsets(nsm_model* model, int* node_offsets, int* elem_offsets); /* [S+1] each */
 int nsm_ensemble_time_steps(nsm_model* model, double* dt);                      /* [S] critical steps */
 /* Per-sample max |field component| over the listed (global) node ids, out [S]
@@ -157,11 +180,11 @@ int nsm_get_ip_data(nsm_model* model, double* F, double* sigma);
 /* Derived element output of the current configuration (replaces
  * Block::ComputeDerivedElementData, src/nimble_block.cc:438-497, through
  * HexElement::ComputeVolumeAverage, src/nimble_element.cc:262-282): element
- * volume [E] and volume-averaged stress [E][6] (weights det J of the current
- * configuration X + u), from the point stresses of the last evaluation that
- * stored point data.  Same operations in the same order as the reference.
- * Either output may be NULL. */
-int nsm_compute_derived_element_data(nsm_model* model, double* volume, double* stress);
+ * volume [E], volume-averaged stress [E][6] and deformation gradient [E][9]
+ * (reference component orders; weights det J of the current configuration
+ * X + u), from the point data of the last evaluation that stored it.  Same
+ * operations in the same order as the reference.  Any output may be NULL. */
+int nsm_compute_derived_element_data(nsm_model* model, double* volume, double* stress, double* deformation_gradient);
 
 /* Kinetic energy 1/2 sum m v.v and internal energy sum det(J_X) W(F) over the
  * integration points (not in the reference; used for energy balance). */
@@ -292,6 +315,13 @@ int nsm_tc_selftest(int N, int K, const float* A, const float* B, float* D);
  * out, after which the kernel freed its tensor memory and returned.  The
  * context stays usable. */
 int nsm_tc_wait_timeout_selftest(long polls, int* timed_out);
+
+/* Diagnostic: the measured FP64 FMA rate of the device in TFLOP/s (16
+ * independent DFMA chains per thread, 64 warps per SM, best of 3 timed
+ * launches), the roof of the FP64 element kernel. */
+int nsm_fp64_peak_probe(int device, double* tflops);
+/* Number of SMs of the device. */
+int nsm_device_sm_count(int device, int* count);
 
 /* Pinned host memory for the host-buffer entry points (page-locked so that the
  * copies run at full link bandwidth). */

@@ -87,11 +87,13 @@ __device__ __forceinline__ void element_work(const ElementArgs& a, const int e)
 #pragma unroll
         for (int t = 0; t < 2; t++) S[d][i][s][t] = T(0);
 
-  T K = T(a.bulk), Gm = T(a.shear);
+  T   K = T(a.bulk), Gm = T(a.shear);
+  int model = a.model;
   if (a.elem_group) {
     const GroupMaterial& m = a.mats[__ldg(&a.elem_group[e])];
     K                      = T(m.bulk);
     Gm                     = T(m.shear);
+    model                  = m.model;
   }
   bool    bad = false;
   T*      rec = reinterpret_cast<T*>(a.ip) + (size_t)e * kIpRecord;
@@ -126,7 +128,7 @@ __device__ __forceinline__ void element_work(const ElementArgs& a, const int e)
         H[i][J] = h;
       }
     T sig[6], C[3][3], J;
-    neohookean<T>(H, K, Gm, sig, C, J);
+    material_stress<T>(model, H, K, Gm, sig, C, J);
     if (!(J > T(0)) || !(det0 > T(0))) bad = true;  // inverted element
     if (store) {
       T r[kIpRecord];
@@ -260,6 +262,7 @@ __global__ void __launch_bounds__(128) k_energy_partials(int N, long ld_n, const
     nodal_gradient<double>(x, Gu);
     const GroupMaterial& mat = mats[elem_group ? elem_group[e] : 0];
     const double         K = mat.bulk, Gm = mat.shear;
+    const bool           elastic_model = mat.model == kElastic;
 #pragma unroll 1
     for (int p = 0; p < 8; p++) {
       const int bit[3] = {sx_of(p), sy_of(p), sz_of(p)};
@@ -275,7 +278,7 @@ __global__ void __launch_bounds__(128) k_energy_partials(int N, long ld_n, const
           }
           H[i][J] = h;
         }
-      ie += geo[(p * 10 + 9) * ld_e + e] * energy_density(H, K, Gm);
+      ie += geo[(p * 10 + 9) * ld_e + e] * (elastic_model ? energy_density_elastic(H, K, Gm) : energy_density(H, K, Gm));
     }
   }
   s_ke[threadIdx.x] = ke;

@@ -150,6 +150,49 @@ __device__ __forceinline__ void neohookean(const T H[3][3], T K, T G, T sig[6], 
   sig[5]      = Gr5 * B[5];
 }
 
+// Small-strain elastic stress (ElasticMaterial::GetStress,
+// src/nimble_material.cc:98-126): eps = sym(F) - I on the unrotated F,
+// sigma = 2 mu eps + lambda tr(eps) I with lambda = K - 2 mu / 3.  From
+// H = F - I the strain is sym(H), without the cancellation of F_ii - 1.
+// Also returns cof(F) and J = det F for the force and the inversion check.
+template <typename T>
+__device__ __forceinline__ void elastic(const T H[3][3], T K, T G, T sig[6], T C[3][3], T& J)
+{
+  T F[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int k = 0; k < 3; k++) F[i][k] = (i == k) ? T(1) + H[i][k] : H[i][k];
+  C[0][0] = F[1][1] * F[2][2] - F[1][2] * F[2][1];
+  C[0][1] = F[1][2] * F[2][0] - F[1][0] * F[2][2];
+  C[0][2] = F[1][0] * F[2][1] - F[1][1] * F[2][0];
+  C[1][0] = F[0][2] * F[2][1] - F[0][1] * F[2][2];
+  C[1][1] = F[0][0] * F[2][2] - F[0][2] * F[2][0];
+  C[1][2] = F[0][1] * F[2][0] - F[0][0] * F[2][1];
+  C[2][0] = F[0][1] * F[1][2] - F[0][2] * F[1][1];
+  C[2][1] = F[0][2] * F[1][0] - F[0][0] * F[1][2];
+  C[2][2] = F[0][0] * F[1][1] - F[0][1] * F[1][0];
+  J       = F[0][0] * C[0][0] + F[0][1] * C[0][1] + F[0][2] * C[0][2];
+  const T two_mu = T(2) * G, lambda = K - T(2) * G / T(3);
+  const T tr     = H[0][0] + H[1][1] + H[2][2];
+  sig[0]         = two_mu * H[0][0] + lambda * tr;
+  sig[1]         = two_mu * H[1][1] + lambda * tr;
+  sig[2]         = two_mu * H[2][2] + lambda * tr;
+  sig[3]         = G * (H[0][1] + H[1][0]);
+  sig[4]         = G * (H[1][2] + H[2][1]);
+  sig[5]         = G * (H[2][0] + H[0][2]);
+}
+
+// The stress of the element's material model.
+template <typename T>
+__device__ __forceinline__ void material_stress(int model, const T H[3][3], T K, T G, T sig[6], T C[3][3], T& J)
+{
+  if (model == kElastic)
+    elastic<T>(H, K, G, sig, C, J);
+  else
+    neohookean<T>(H, K, G, sig, C, J);
+}
+
 template <typename T>
 __device__ __forceinline__ T sym(const T s[6], int i, int k)
 {
@@ -202,6 +245,23 @@ __device__ __forceinline__ double energy_density(const double H[3][3], double K,
   double vol   = 0.25 * K * (Jm1 * (Jm1 + 2.0)) - 0.5 * K * lnJ;
   double iso   = 0.5 * G * (3.0 * expm1(-2.0 / 3.0 * lnJ) + Jm23 * trbm3);
   return vol + iso;
+}
+
+// Strain energy density of the small-strain elastic material:
+// W = mu eps:eps + lambda/2 tr(eps)^2, eps = sym(H), whose stress is elastic().
+__device__ __forceinline__ double energy_density_elastic(const double H[3][3], double K, double G)
+{
+  const double lambda = K - 2.0 * G / 3.0;
+  const double tr     = H[0][0] + H[1][1] + H[2][2];
+  double       ee     = 0.0;
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      const double e = 0.5 * (H[i][k] + H[k][i]);
+      ee += e * e;
+    }
+  return G * ee + 0.5 * lambda * tr * tr;
 }
 
 }  // namespace nsm

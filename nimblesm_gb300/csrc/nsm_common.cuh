@@ -12,6 +12,11 @@
 
 namespace nsm {
 
+// Material models (the reference's MaterialFactory names,
+// src/nimble_material_factory.cc:57-70).
+constexpr int kNeohookean = 0;  // "neohookean", src/nimble_material.cc:252-310
+constexpr int kElastic    = 1;  // "elastic", src/nimble_material.cc:98-126
+
 // Natural coordinate of the Gauss points (src/nimble_element.cc:58).
 constexpr double kGauss = 0.577350269189626;
 

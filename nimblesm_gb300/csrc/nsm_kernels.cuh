@@ -12,17 +12,20 @@
 
 namespace nsm {
 
-// Material of one sample of an ensemble (one entry for a single mesh).
+// One material: of a block of a multi-block mesh, or of one sample of an
+// ensemble (one entry for a single mesh).
 struct GroupMaterial {
   double bulk, shear, density, sound_speed;
+  int    model;
+  int    pad;
 };
 
 struct SetupArgs {
   int           N, E;
   int           num_groups;      // samples; elements of sample g are [elem_off[g], elem_off[g+1])
-  const int*    elem_group;      // [E] sample of each element (null: one sample)
+  const int*    elem_group;      // [E] material of each element (null: material 0)
   const int*    elem_off;        // [num_groups+1]
-  const GroupMaterial* mats;     // [num_groups]
+  const GroupMaterial* mats;     // materials
   long          ld_n, ld_e;
   const int*    conn;      // [8][ld_e]
   const double* X;         // [3][ld_n]
@@ -41,11 +44,12 @@ struct SetupArgs {
 void        shape_tables(double* N, double* dN);
 cudaError_t upload_shape_tables(cudaStream_t stream);
 cudaError_t launch_setup(const SetupArgs& a, cudaStream_t stream);
-// Element volume [E] and volume-averaged stress [E][6] of the current
-// configuration from the point records (setup_kernels.cu).
+// Element volume [E], volume-averaged stress [E][6] and deformation
+// gradient [E][9] of the current configuration from the point records
+// (setup_kernels.cu).
 cudaError_t launch_derived_element(int E, long ld_e, const int* conn, const double* X, const double* u, long ld_n,
-                                   const void* ip, int ip_is_float, double* volume, double* avg, int* status,
-                                   cudaStream_t stream);
+                                   const void* ip, int ip_is_float, double* volume, double* avg_sigma, double* avg_F,
+                                   int* status, cudaStream_t stream);
 
 // Per-point record of the element data: 16 values of type T per element and
 // integration point, records laid out [ip][ld_e][16]: slots 0..8 F in the
@@ -64,9 +68,10 @@ struct ElementArgs {
   const float*  Xf;        // [3][ld_n] FP32 copy of X (FP32 form)
   const double* geo;       // [80][ld_e] G0 and det J0 per ip (FP64 form only)
   double        bulk, shear;     // material when elem_group is null
-  const int*    elem_group;      // [E] sample of each element, or null
-  const GroupMaterial* mats;     // [num_groups]
-  int           num_groups;
+  int           model;           // material model when elem_group is null
+  const int*    elem_group;      // [E] material of each element, or null
+  const GroupMaterial* mats;     // materials
+  int           num_groups;      // samples (rows of the schedule)
   int           persistent;      // 0: one thread per element; 1: grid-stride over elements
   void*         ip;        // [8][ld_e][16] per-point records (T)
   void*         fe;        // [ld_e][24] element nodal forces, corner-major (T)

@@ -53,7 +53,8 @@ struct nsm_model {
   std::vector<int> node_off, elem_off;  // per-sample offsets [S+1]
   long         ld_n = 0, ld_e = 0;
   int          precision = NSM_PRECISION_FP64, store_ip = 1, graph_steps = 50, device = 0;
-  double       density = 0, K = 0, G = 0, dt_crit = 0;
+  double       density = 0, K = 0, G = 0, dt_crit = 0;  // material 0
+  int          model = NSM_MATERIAL_NEOHOOKEAN, num_mats = 1;
   cudaStream_t stream = nullptr;
 
   int*    d_conn = nullptr;  // [8][ld_e]
@@ -78,10 +79,10 @@ struct nsm_model {
   double* d_stage = nullptr;    // [3N] AoS staging for host copies
   double* d_out = nullptr;      // small results
   double* d_group_out = nullptr;// [S] per-sample results
-  int*    d_elem_group = nullptr;  // [E] sample of each element (S > 1)
+  int*    d_elem_group = nullptr;  // [E] material of each element (more than one material)
   int*    d_node_group = nullptr;  // [N] sample of each node (S > 1)
   int*    d_elem_off = nullptr;    // [S+1]
-  nsm::GroupMaterial* d_mats = nullptr;  // [S]
+  nsm::GroupMaterial* d_mats = nullptr;  // [num_mats]
   std::vector<double> dt_group;    // per-sample critical time step
   nsm::ElementLaunch  elaunch{128, 0, 0};
   nsm_mlp*            closure = nullptr;        // learned material (FP32 form), or null
@@ -218,6 +219,7 @@ nsm::ElementArgs element_args(nsm_model* m, int k)
   a.geo       = m->d_geo;
   a.bulk      = m->K;
   a.shear     = m->G;
+  a.model     = m->model;
   a.ip        = m->d_ip;
   a.fe        = m->d_fe;
   a.elem_group = m->d_elem_group;
@@ -352,21 +354,29 @@ int         nsm_abi_version(void) { return NSM_ABI_VERSION; }
 namespace {
 
 // One handle over S samples: the samples' meshes are concatenated (node and
-// element ids offset per sample), each element carries its sample's material
-// and each node its sample's time schedule.  A single mesh is S = 1.
-int create_impl(int S, const nsm_mesh_desc* meshes, const nsm_neohookean* materials, const nsm_options* options,
-                nsm_model** out)
+// element ids offset per sample) and each node carries its sample's time
+// schedule.  Materials: `num_mats` entries, element e uses
+// materials[elem_mat[e]] (global element ids); elem_mat null means material
+// g for the elements of sample g when num_mats == S (ensembles), or material
+// 0 (one material).  A single mesh is S = 1.
+int create_impl(int S, const nsm_mesh_desc* meshes, int num_mats, const nsm_material* materials,
+                const int* elem_mat, const nsm_options* options, nsm_model** out)
 {
-  if (!meshes || !materials || !out || S < 1) return fail(NSM_ERR_INVALID_ARGUMENT, "null argument");
+  if (!meshes || !materials || !out || S < 1 || num_mats < 1) return fail(NSM_ERR_INVALID_ARGUMENT, "null argument");
+  if (!elem_mat && num_mats != 1 && num_mats != S) return fail(NSM_ERR_INVALID_ARGUMENT, "materials per element needed");
   *out = nullptr;
+  for (int b = 0; b < num_mats; b++) {
+    const nsm_material& mat = materials[b];
+    if (mat.model != NSM_MATERIAL_NEOHOOKEAN && mat.model != NSM_MATERIAL_ELASTIC)
+      return fail(NSM_ERR_INVALID_ARGUMENT, "unknown material model");
+    if (!(mat.density > 0) || !(mat.bulk_modulus > 0) || !(mat.shear_modulus >= 0))
+      return fail(NSM_ERR_INVALID_ARGUMENT, "invalid material parameters");
+  }
   std::vector<int> node_off(S + 1, 0), elem_off(S + 1, 0);
   for (int g = 0; g < S; g++) {
     const nsm_mesh_desc& mesh = meshes[g];
     if (mesh.num_nodes < 0 || mesh.num_elem < 0 || (mesh.num_elem > 0 && (!mesh.coords || !mesh.conn)))
       return fail(NSM_ERR_INVALID_ARGUMENT, "invalid mesh");
-    const nsm_neohookean& mat = materials[g];
-    if (!(mat.density > 0) || !(mat.bulk_modulus > 0) || !(mat.shear_modulus >= 0))
-      return fail(NSM_ERR_INVALID_ARGUMENT, "invalid neo-Hookean parameters");
     for (long i = 0; i < 8L * mesh.num_elem; i++)
       if (mesh.conn[i] < 0 || mesh.conn[i] >= mesh.num_nodes)
         return fail(NSM_ERR_INVALID_ARGUMENT, "connectivity out of range");
@@ -376,6 +386,15 @@ int create_impl(int S, const nsm_mesh_desc* meshes, const nsm_neohookean* materi
     elem_off[g + 1] = elem_off[g] + mesh.num_elem;
   }
   const int N = node_off[S], E = elem_off[S];
+  if (elem_mat) {
+    // materials of a multi-block mesh: blocks are contiguous in element order,
+    // which is the reference's block-by-block assembly order
+    for (int e = 0; e < E; e++) {
+      if (elem_mat[e] < 0 || elem_mat[e] >= num_mats) return fail(NSM_ERR_INVALID_ARGUMENT, "block index out of range");
+      if (e > 0 && elem_mat[e] < elem_mat[e - 1])
+        return fail(NSM_ERR_INVALID_ARGUMENT, "elements must be ordered by block");
+    }
+  }
 
   nsm_model* m = new nsm_model();
   m->N = N;
@@ -395,13 +414,15 @@ int create_impl(int S, const nsm_mesh_desc* meshes, const nsm_neohookean* materi
     delete m;
     return fail(NSM_ERR_INVALID_ARGUMENT, "unknown precision");
   }
-  m->density = materials[0].density;
-  m->K       = materials[0].bulk_modulus;
-  m->G       = materials[0].shear_modulus;
-  std::vector<nsm::GroupMaterial> gm(S);
-  for (int g = 0; g < S; g++)
-    gm[g] = nsm::GroupMaterial{materials[g].bulk_modulus, materials[g].shear_modulus, materials[g].density,
-                               std::sqrt(materials[g].bulk_modulus / materials[g].density)};
+  m->density   = materials[0].density;
+  m->K         = materials[0].bulk_modulus;
+  m->G         = materials[0].shear_modulus;
+  m->model     = materials[0].model;
+  m->num_mats  = num_mats;
+  std::vector<nsm::GroupMaterial> gm(num_mats);
+  for (int b = 0; b < num_mats; b++)
+    gm[b] = nsm::GroupMaterial{materials[b].bulk_modulus, materials[b].shear_modulus, materials[b].density,
+                               std::sqrt(materials[b].bulk_modulus / materials[b].density), materials[b].model, 0};
 
   auto bail = [&](int code) {
     free_all(m);
@@ -444,8 +465,9 @@ int create_impl(int S, const nsm_mesh_desc* meshes, const nsm_neohookean* materi
   NSM_CUDA_B(cudaMalloc(&m->d_out, sizeof(double) * 8));
   NSM_CUDA_B(cudaMalloc(&m->d_group_out, sizeof(double) * S));
   NSM_CUDA_B(cudaMalloc(&m->d_stage, nb));
-  NSM_CUDA_B(cudaMalloc(&m->d_mats, sizeof(nsm::GroupMaterial) * S));
-  NSM_CUDA_B(cudaMemcpyAsync(m->d_mats, gm.data(), sizeof(nsm::GroupMaterial) * S, cudaMemcpyHostToDevice, m->stream));
+  NSM_CUDA_B(cudaMalloc(&m->d_mats, sizeof(nsm::GroupMaterial) * num_mats));
+  NSM_CUDA_B(cudaMemcpyAsync(m->d_mats, gm.data(), sizeof(nsm::GroupMaterial) * num_mats, cudaMemcpyHostToDevice,
+                             m->stream));
   NSM_CUDA_B(cudaMalloc(&m->d_elem_off, sizeof(int) * (S + 1)));
   NSM_CUDA_B(cudaMemcpyAsync(m->d_elem_off, elem_off.data(), sizeof(int) * (S + 1), cudaMemcpyHostToDevice, m->stream));
   size_t scratch = sizeof(double) * (E > 0 ? (size_t)E : 1);
@@ -457,10 +479,8 @@ int create_impl(int S, const nsm_mesh_desc* meshes, const nsm_neohookean* materi
     std::vector<int>    conn_soa((size_t)8 * m->ld_e, 0);
     std::vector<double> X((size_t)3 * m->ld_n, 0.0);
     std::vector<int>    egroup, ngroup;
-    if (S > 1) {
-      egroup.resize(E);
-      ngroup.resize(N);
-    }
+    if (num_mats > 1) egroup.resize(E);
+    if (S > 1) ngroup.resize(N);
     std::vector<int> gconn((size_t)8 * E);
     for (int g = 0; g < S; g++) {
       const nsm_mesh_desc& mesh = meshes[g];
@@ -471,7 +491,7 @@ int create_impl(int S, const nsm_mesh_desc* meshes, const nsm_neohookean* materi
           conn_soa[(size_t)c * m->ld_e + ge] = gid;
           gconn[8 * ge + c]                = gid;
         }
-        if (S > 1) egroup[ge] = g;
+        if (num_mats > 1) egroup[ge] = elem_mat ? elem_mat[ge] : g;
       }
       for (long n = 0; n < mesh.num_nodes; n++) {
         long gn = node_off[g] + n;
@@ -494,11 +514,13 @@ int create_impl(int S, const nsm_mesh_desc* meshes, const nsm_neohookean* materi
     if (E > 0)
       NSM_CUDA_B(cudaMemcpyAsync(m->d_node_inc, inc.data(), sizeof(int) * inc.size(), cudaMemcpyHostToDevice,
                                  m->stream));
-    if (S > 1) {
+    if (num_mats > 1) {
       NSM_CUDA_B(cudaMalloc(&m->d_elem_group, sizeof(int) * (E > 0 ? E : 1)));
-      NSM_CUDA_B(cudaMalloc(&m->d_node_group, sizeof(int) * (N > 0 ? N : 1)));
       if (E > 0)
         NSM_CUDA_B(cudaMemcpyAsync(m->d_elem_group, egroup.data(), sizeof(int) * E, cudaMemcpyHostToDevice, m->stream));
+    }
+    if (S > 1) {
+      NSM_CUDA_B(cudaMalloc(&m->d_node_group, sizeof(int) * (N > 0 ? N : 1)));
       if (N > 0)
         NSM_CUDA_B(cudaMemcpyAsync(m->d_node_group, ngroup.data(), sizeof(int) * N, cudaMemcpyHostToDevice, m->stream));
     }
@@ -552,16 +574,33 @@ int create_impl(int S, const nsm_mesh_desc* meshes, const nsm_neohookean* materi
 
 extern "C" {
 
+static nsm_material as_material(const nsm_neohookean& m)
+{
+  return nsm_material{NSM_MATERIAL_NEOHOOKEAN, 0, m.density, m.bulk_modulus, m.shear_modulus};
+}
+
 int nsm_create(const nsm_mesh_desc* mesh, const nsm_neohookean* material, const nsm_options* options,
                nsm_model** out)
 {
-  return create_impl(1, mesh, material, options, out);
+  if (!material) return fail(NSM_ERR_INVALID_ARGUMENT, "null argument");
+  const nsm_material mat = as_material(*material);
+  return create_impl(1, mesh, 1, &mat, nullptr, options, out);
 }
 
 int nsm_create_ensemble(int num_samples, const nsm_mesh_desc* meshes, const nsm_neohookean* materials,
                         const nsm_options* options, nsm_model** out)
 {
-  return create_impl(num_samples, meshes, materials, options, out);
+  if (!materials || num_samples < 1) return fail(NSM_ERR_INVALID_ARGUMENT, "null argument");
+  std::vector<nsm_material> mats(num_samples);
+  for (int g = 0; g < num_samples; g++) mats[g] = as_material(materials[g]);
+  return create_impl(num_samples, meshes, num_samples, mats.data(), nullptr, options, out);
+}
+
+int nsm_create_blocks(const nsm_mesh_desc* mesh, int num_blocks, const int* elem_block, const nsm_material* materials,
+                      const nsm_options* options, nsm_model** out)
+{
+  if (!mesh || num_blocks < 1 || (num_blocks > 1 && !elem_block)) return fail(NSM_ERR_INVALID_ARGUMENT, "null argument");
+  return create_impl(1, mesh, num_blocks, materials, num_blocks > 1 ? elem_block : nullptr, options, out);
 }
 
 int nsm_ensemble_offsets(nsm_model* m, int* node_offsets, int* elem_offsets)
@@ -746,20 +785,22 @@ int nsm_get_ip_data(nsm_model* m, double* F, double* sigma)
   return NSM_OK;
 }
 
-int nsm_compute_derived_element_data(nsm_model* m, double* volume, double* stress)
+int nsm_compute_derived_element_data(nsm_model* m, double* volume, double* stress, double* deformation_gradient)
 {
   if (!m) return fail(NSM_ERR_INVALID_ARGUMENT, "null model");
   NSM_CUDA(cudaSetDevice(m->device));
   if (m->E == 0) return NSM_OK;
-  const int is_float = m->precision == NSM_PRECISION_FP64 ? 0 : 1;
-  double*   tmp      = nullptr;
-  NSM_CUDA(cudaMalloc(&tmp, sizeof(double) * 7 * (size_t)m->E));
+  const int    is_float = m->precision == NSM_PRECISION_FP64 ? 0 : 1;
+  const size_t E        = (size_t)m->E;
+  double*      tmp      = nullptr;
+  NSM_CUDA(cudaMalloc(&tmp, sizeof(double) * 16 * E));
   cudaError_t e = nsm::launch_derived_element(m->E, m->ld_e, m->d_conn, m->d_X, m->d_u, m->ld_n, m->d_ip, is_float,
-                                              tmp, tmp + m->E, m->d_status, m->stream);
-  if (e == cudaSuccess && volume)
-    e = cudaMemcpyAsync(volume, tmp, sizeof(double) * (size_t)m->E, cudaMemcpyDeviceToHost, m->stream);
+                                              tmp, tmp + E, tmp + 7 * E, m->d_status, m->stream);
+  if (e == cudaSuccess && volume) e = cudaMemcpyAsync(volume, tmp, sizeof(double) * E, cudaMemcpyDeviceToHost, m->stream);
   if (e == cudaSuccess && stress)
-    e = cudaMemcpyAsync(stress, tmp + m->E, sizeof(double) * 6 * (size_t)m->E, cudaMemcpyDeviceToHost, m->stream);
+    e = cudaMemcpyAsync(stress, tmp + E, sizeof(double) * 6 * E, cudaMemcpyDeviceToHost, m->stream);
+  if (e == cudaSuccess && deformation_gradient)
+    e = cudaMemcpyAsync(deformation_gradient, tmp + 7 * E, sizeof(double) * 9 * E, cudaMemcpyDeviceToHost, m->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(m->stream);
   cudaFree(tmp);
   if (e != cudaSuccess) return cuda_fail(e, "nsm_compute_derived_element_data");
@@ -985,7 +1026,8 @@ int nsm_set_mlp_closure(nsm_model* m, nsm_mlp* closure)
   if (!m) return fail(NSM_ERR_INVALID_ARGUMENT, "null model");
   if (closure) {
     if (m->precision != NSM_PRECISION_FP32_MIXED) return fail(NSM_ERR_INVALID_ARGUMENT, "the learned closure runs in the FP32-mixed form");
-    if (m->S != 1) return fail(NSM_ERR_INVALID_ARGUMENT, "the learned closure is trained for one material");
+    if (m->S != 1 || m->num_mats != 1 || m->model != NSM_MATERIAL_NEOHOOKEAN)
+      return fail(NSM_ERR_INVALID_ARGUMENT, "the learned closure is trained for one neo-Hookean material");
     double K = 0, G = 0;
     nsm::mlp::MlpElementArgs ma;
     nsm::mlp::element_args(closure, &ma, &K, &G);

@@ -197,14 +197,16 @@ __global__ void k_min_reduce(long n, const double* __restrict__ in, double* __re
 // src/nimble_element.cc:262-282 and src/nimble_element.h:343-392): the
 // current coordinates x = X + u, at each point the current Jacobian
 // sum_n (x_n + 0) (x) dN_n/dxi and its determinant (Invert3x3), the element
-// volume sum_p det_p and the volume-averaged stress sum_p (sigma_p w_p) det_p
-// / volume, w_p = 1.  The operations and their order are the reference's and
+// volume sum_p det_p and the volume averages sum_p (q_p w_p) det_p / volume,
+// w_p = 1, of the stress and the deformation gradient (each component on its
+// own, as the reference averages every requested element field).  The operations and their order are the reference's and
 // this file is compiled without FMA contraction, so for the same u and
 // point stresses the result is the reference's bit for bit.
 template <typename TR>
 __global__ void k_derived_element(int E, long ld_e, const int* __restrict__ conn, const double* __restrict__ X,
                                   const double* __restrict__ u, long ld_n, const TR* __restrict__ ip,
-                                  double* __restrict__ volume, double* __restrict__ avg, int* __restrict__ status)
+                                  double* __restrict__ volume, double* __restrict__ avg_sigma,
+                                  double* __restrict__ avg_F, int* __restrict__ status)
 {
   int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= E) return;
@@ -215,7 +217,9 @@ __global__ void k_derived_element(int E, long ld_e, const int* __restrict__ conn
 #pragma unroll
     for (int k = 0; k < 3; k++) x[n][k] = X[k * ld_n + id] + u[k * ld_n + id];
   }
-  double vol = 0.0, acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  double vol = 0.0, acc[15];  // F slots 0-8, sigma 9-14 (the record's order)
+#pragma unroll
+  for (int q = 0; q < 15; q++) acc[q] = 0.0;
   bool   bad = false;
 #pragma unroll 1
   for (int p = 0; p < 8; p++) {
@@ -239,25 +243,27 @@ __global__ void k_derived_element(int E, long ld_e, const int* __restrict__ conn
     vol += det;
     const TR* rec = ip + ((size_t)p * ld_e + e) * kIpRecord;
 #pragma unroll
-    for (int q = 0; q < 6; q++) acc[q] += (double)rec[9 + q] * 1.0 * det;
+    for (int q = 0; q < 15; q++) acc[q] += (double)rec[q] * 1.0 * det;
   }
 #pragma unroll
-  for (int q = 0; q < 6; q++) avg[6 * (size_t)e + q] = acc[q] / vol;
+  for (int q = 0; q < 6; q++) avg_sigma[6 * (size_t)e + q] = acc[9 + q] / vol;
+#pragma unroll
+  for (int q = 0; q < 9; q++) avg_F[9 * (size_t)e + q] = acc[q] / vol;
   volume[e] = vol;
   if (bad) atomicOr(status, NSM_STATUS_BAD_JACOBIAN);
 }
 
 cudaError_t launch_derived_element(int E, long ld_e, const int* conn, const double* X, const double* u, long ld_n,
-                                   const void* ip, int ip_is_float, double* volume, double* avg, int* status,
-                                   cudaStream_t stream)
+                                   const void* ip, int ip_is_float, double* volume, double* avg_sigma, double* avg_F,
+                                   int* status, cudaStream_t stream)
 {
   if (E == 0) return cudaSuccess;
   if (ip_is_float)
     k_derived_element<float><<<grid_for(E, 128), 128, 0, stream>>>(E, ld_e, conn, X, u, ld_n, (const float*)ip, volume,
-                                                                   avg, status);
+                                                                   avg_sigma, avg_F, status);
   else
     k_derived_element<double><<<grid_for(E, 128), 128, 0, stream>>>(E, ld_e, conn, X, u, ld_n, (const double*)ip,
-                                                                     volume, avg, status);
+                                                                     volume, avg_sigma, avg_F, status);
   return cudaGetLastError();
 }
 

@@ -43,6 +43,11 @@ class _Material(C.Structure):
     _fields_ = [("density", C.c_double), ("bulk_modulus", C.c_double), ("shear_modulus", C.c_double)]
 
 
+class _AnyMaterial(C.Structure):
+    _fields_ = [("model", C.c_int), ("reserved", C.c_int), ("density", C.c_double), ("bulk_modulus", C.c_double),
+                ("shear_modulus", C.c_double)]
+
+
 class _Options(C.Structure):
     _fields_ = [("precision", C.c_int), ("store_ip_data", C.c_int), ("device", C.c_int),
                 ("graph_steps", C.c_int)]
@@ -58,6 +63,8 @@ SIGNATURES = {
     "nsm_last_error": (C.c_char_p, []),
     "nsm_abi_version": (C.c_int, []),
     "nsm_create": (C.c_int, [C.POINTER(_Mesh), C.POINTER(_Material), C.POINTER(_Options), C.POINTER(_vp)]),
+    "nsm_create_blocks": (C.c_int, [C.POINTER(_Mesh), C.c_int, _ip, C.POINTER(_AnyMaterial), C.POINTER(_Options),
+                                    C.POINTER(_vp)]),
     "nsm_destroy": (C.c_int, [_vp]),
     "nsm_add_boundary_condition": (C.c_int, [_vp, C.c_int, C.c_int, C.c_double, _ip, C.c_int]),
     "nsm_compute_lumped_mass": (C.c_int, [_vp, _dp]),
@@ -69,7 +76,7 @@ SIGNATURES = {
     "nsm_compute_internal_force": (C.c_int, [_vp, C.c_double, C.c_double, C.c_int]),
     "nsm_compute_internal_force_host": (C.c_int, [_vp, _dp, _dp]),
     "nsm_get_ip_data": (C.c_int, [_vp, _dp, _dp]),
-    "nsm_compute_derived_element_data": (C.c_int, [_vp, _dp, _dp]),
+    "nsm_compute_derived_element_data": (C.c_int, [_vp, _dp, _dp, _dp]),
     "nsm_get_energies": (C.c_int, [_vp, _dp, _dp]),
     "nsm_begin": (C.c_int, [_vp, C.c_double, C.c_double, C.c_int, C.c_int, _dp]),
     "nsm_advance": (C.c_int, [_vp, C.c_int]),
@@ -104,6 +111,8 @@ SIGNATURES = {
     "nsm_closure_fallbacks": (C.c_int, [_vp, C.POINTER(C.c_ulonglong)]),
     "nsm_tc_selftest": (C.c_int, [C.c_int, C.c_int, _dp_f, _dp_f, _dp_f]),
     "nsm_tc_wait_timeout_selftest": (C.c_int, [C.c_long, C.POINTER(C.c_int)]),
+    "nsm_fp64_peak_probe": (C.c_int, [C.c_int, _dp]),
+    "nsm_device_sm_count": (C.c_int, [C.c_int, C.POINTER(C.c_int)]),
     "nsm_host_alloc": (_vp, [C.c_size_t]),
     "nsm_host_free": (None, [_vp]),
 }
@@ -175,7 +184,19 @@ class Model:
             mats[g] = _Material(p.density, p.bulk_modulus, p.shear_modulus)
         opt = _Options(PRECISION[precision], 1 if store_ip_data else 0, device, graph_steps)
         h = _vp()
-        if len(problems) == 1:
+        single = problems[0]
+        if len(problems) == 1 and (single.blocks or single.material_model != "neohookean"):
+            blocks = single.materials()
+            bm = (_AnyMaterial * len(blocks))()
+            for b, mt in enumerate(blocks):
+                bm[b] = _AnyMaterial(mt.MODELS[mt.model], 0, mt.density, mt.bulk_modulus, mt.shear_modulus)
+            eb = None
+            if len(blocks) > 1:
+                eb = np.ascontiguousarray(single.elem_block, dtype=np.int32)
+                keep.append(eb)
+            _check(lib.nsm_create_blocks(meshes, len(blocks), eb.ctypes.data_as(_ip) if eb is not None else None,
+                                         bm, C.byref(opt), C.byref(h)))
+        elif len(problems) == 1:
             _check(lib.nsm_create(meshes, mats, C.byref(opt), C.byref(h)))
         else:
             _check(lib.nsm_create_ensemble(len(problems), meshes, mats, C.byref(opt), C.byref(h)))
@@ -243,12 +264,13 @@ class Model:
         return F, s
 
     def ComputeDerivedElementData(self):
-        """Element volume [E] and volume-averaged stress [E][6] of the current
-        configuration (Block::ComputeDerivedElementData)."""
+        """Element volume [E], volume-averaged stress [E][6] and deformation
+        gradient [E][9] of the current configuration
+        (Block::ComputeDerivedElementData)."""
         E = self.problem.num_elem
-        vol, s = np.zeros(E), np.zeros((E, 6))
-        _check(library().nsm_compute_derived_element_data(self._h, _d(vol), _d(s)))
-        return vol, s
+        vol, s, F = np.zeros(E), np.zeros((E, 6)), np.zeros((E, 9))
+        _check(library().nsm_compute_derived_element_data(self._h, _d(vol), _d(s), _d(F)))
+        return vol, s, F
 
     def GetEnergies(self):
         ke, ie = C.c_double(), C.c_double()
@@ -429,6 +451,19 @@ def _concatenate(problems):
     return Problem(coords=coords, conn=conn, node_sets={}, density=problems[0].density,
                    bulk_modulus=problems[0].bulk_modulus, shear_modulus=problems[0].shear_modulus, bcs=[],
                    v_init=v0)
+
+
+def fp64_peak_tflops(device=0):
+    """Measured FP64 FMA rate of the device (TFLOP/s)."""
+    t = C.c_double(0.0)
+    _check(library().nsm_fp64_peak_probe(device, C.byref(t)))
+    return t.value
+
+
+def device_sm_count(device=0):
+    n = C.c_int(0)
+    _check(library().nsm_device_sm_count(device, C.byref(n)))
+    return n.value
 
 
 def run(problem: Problem, final_time: float, num_steps: int, output_frequency: int = 0,

@@ -61,9 +61,29 @@ class BoundaryCondition:
         return f"{kind} {self.node_set} {'xyz'[self.component]} {self.value!r}"
 
 
+class Material:
+    """One material line of an input deck: "<model> density .. bulk_modulus ..
+    shear_modulus ..", model "neohookean" or "elastic"."""
+
+    MODELS = {"neohookean": 0, "elastic": 1}
+
+    def __init__(self, model: str, density: float, bulk_modulus: float, shear_modulus: float):
+        if model not in self.MODELS:
+            raise ValueError(f"unknown material model {model!r}")
+        self.model, self.density = model, float(density)
+        self.bulk_modulus, self.shear_modulus = float(bulk_modulus), float(shear_modulus)
+
+    def line(self) -> str:
+        return (f"{self.model} density {self.density!r} bulk_modulus {self.bulk_modulus!r} "
+                f"shear_modulus {self.shear_modulus!r}")
+
+
 @dataclass
 class Problem:
-    """An explicit-dynamics problem on one block of hex8 elements."""
+    """An explicit-dynamics problem on hex8 elements: one block with the
+    material (material_model, density, bulk_modulus, shear_modulus), or, with
+    `blocks` and `elem_block`, several element blocks each with its own
+    Material (elements ordered by block)."""
     coords: np.ndarray               # [N,3] float64
     conn: np.ndarray                 # [E,8] int32, 0-based
     node_sets: dict = field(default_factory=dict)   # name -> int32 array of node ids
@@ -72,6 +92,9 @@ class Problem:
     shear_modulus: float = 79.3e9
     bcs: list = field(default_factory=list)         # [BoundaryCondition]
     v_init: np.ndarray | None = None  # [N,3] velocity written after the initial conditions
+    material_model: str = "neohookean"  # "neohookean" | "elastic" (MaterialFactory names)
+    blocks: list | None = None          # [Material] per element block
+    elem_block: np.ndarray | None = None  # [E] block index, non-decreasing
 
     @property
     def num_nodes(self) -> int:
@@ -81,9 +104,14 @@ class Problem:
     def num_elem(self) -> int:
         return int(self.conn.shape[0])
 
+    def materials(self) -> list:
+        """The materials of the blocks (one for a single-block problem)."""
+        if self.blocks:
+            return list(self.blocks)
+        return [Material(self.material_model, self.density, self.bulk_modulus, self.shear_modulus)]
+
     def material_line(self) -> str:
-        return (f"neohookean density {self.density!r} bulk_modulus {self.bulk_modulus!r} "
-                f"shear_modulus {self.shear_modulus!r}")
+        return self.materials()[0].line()
 
     def bc_arrays(self):
         """BCs flattened to (kind[], component[], value[], ptr[], nodes[]) in deck

@@ -369,6 +369,62 @@ nsm_oracle_stress(int n, const double* F, double K, double G, double* sigma)
   for (int p = 0; p < n; p++) neohookean_point(&F[9 * p], K, G, &sigma[6 * p]);
 }
 
+/* ElasticMaterial::GetStress (src/nimble_material.cc:98-126): the strain is
+ * the symmetric part of the unrotated F minus I, in the symmetric slots
+ * xx, yy, zz, xy, yz, zx (K_S_*); F in the full-tensor slots
+ * xx, yy, zz, xy, yz, zx, yx, zy, xz (K_F_*). */
+static void
+elastic_point(const double* F, double K, double G, double* sig)
+{
+  double       strain[6];
+  const double two_mu = 2.0 * G;
+  const double lambda = K - 2.0 * G / 3.0;
+  strain[0]           = F[0] - 1.0;
+  strain[1]           = F[1] - 1.0;
+  strain[2]           = F[2] - 1.0;
+  strain[3]           = 0.5 * (F[3] + F[6]);
+  strain[4]           = 0.5 * (F[4] + F[7]);
+  strain[5]           = 0.5 * (F[5] + F[8]);
+  const double trace  = strain[0] + strain[1] + strain[2];
+  sig[0]              = two_mu * strain[0] + lambda * trace;
+  sig[1]              = two_mu * strain[1] + lambda * trace;
+  sig[2]              = two_mu * strain[2] + lambda * trace;
+  sig[3]              = two_mu * strain[3];
+  sig[4]              = two_mu * strain[4];
+  sig[5]              = two_mu * strain[5];
+}
+
+void
+nsm_oracle_stress_model(int model, int n, const double* F, double K, double G, double* sigma)
+{
+  for (int p = 0; p < n; p++) {
+    if (model == NSM_ORACLE_ELASTIC)
+      elastic_point(&F[9 * p], K, G, &sigma[6 * p]);
+    else
+      neohookean_point(&F[9 * p], K, G, &sigma[6 * p]);
+  }
+}
+
+/* The material of element e: its block's (ModelData keeps one Block and one
+ * Material per element block, src/nimble_model_data.cc:484-493), or the
+ * single material. */
+static void
+material_of(const nsm_oracle_model* m, int e, int* model, double* density, double* K, double* G)
+{
+  if (m->num_blocks > 1 && m->elem_block) {
+    const int b = m->elem_block[e];
+    *model      = m->block_model[b];
+    *density    = m->block_density[b];
+    *K          = m->block_bulk[b];
+    *G          = m->block_shear[b];
+  } else {
+    *model   = m->material_model;
+    *density = m->density;
+    *K       = m->bulk_modulus;
+    *G       = m->shear_modulus;
+  }
+}
+
 /* ComputeNodalForces_impl with the current coordinates passed as the
  * "reference" and zero displacement (src/nimble_element.cc:457-472,
  * src/nimble_element.h:540-625). */
@@ -425,43 +481,46 @@ gather_element(const nsm_oracle_model* m, int e, const double* field, double* ou
 }
 
 /* HexElement::ComputeVolumeAverage (src/nimble_element.cc:262-282) ->
- * ComputeVolumeAverageQuantities_impl (src/nimble_element.h:343-392) for the
- * 6 stress components: the element's coordinates enter as "reference"
- * coordinates plus a zero displacement, the current Jacobian and its
- * determinant come from Invert3x3 at each point, volume = sum det, and the
- * average sums q * w * det with w = 1 before one division by the volume. */
+ * ComputeVolumeAverageQuantities_impl (src/nimble_element.h:343-392) for nq
+ * point quantities (nq <= 32): the element's coordinates enter as
+ * "reference" coordinates plus a zero displacement, the current Jacobian and
+ * its determinant come from Invert3x3 at each point, volume = sum det, and
+ * each average sums q * w * det with w = 1 before one division by the
+ * volume. */
 void
-nsm_oracle_volume_average(const double* x, const double* q, double* volume, double* avg)
+nsm_oracle_volume_average(const double* x, int nq, const double* q, double* volume, double* avg)
 {
   build_tables();
   double cc[24];
   for (int i = 0; i < 24; i++) cc[i] = x[i] + 0.0;
-  double vol = 0.0, acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  double vol = 0.0, acc[32];
+  for (int k = 0; k < nq; k++) acc[k] = 0.0;
   for (int ip = 0; ip < 8; ip++) {
     double a[3][3], a_inv[3][3];
     jacobian(cc, ip, a);
     double det = invert3x3(a, a_inv);
     vol += det;
-    for (int k = 0; k < 6; k++) acc[k] += q[6 * ip + k] * 1.0 * det;
+    for (int k = 0; k < nq; k++) acc[k] += q[nq * ip + k] * 1.0 * det;
   }
-  for (int k = 0; k < 6; k++) avg[k] = acc[k] / vol;
+  for (int k = 0; k < nq; k++) avg[k] = acc[k] / vol;
   *volume = vol;
 }
 
 /* Block::ComputeDerivedElementData (src/nimble_block.cc:438-497): current
- * coordinates X + u per element (:477-483), then the volume average of the
- * element's point stresses. */
+ * coordinates X + u per element (:477-483), then the volume averages of the
+ * element's point stresses and deformation gradients. */
 void
-nsm_oracle_derived_element_data(const nsm_oracle_model* m, const double* u, const double* sigma, double* volume,
-                                double* avg)
+nsm_oracle_derived_element_data(const nsm_oracle_model* m, const double* u, const double* sigma, const double* F,
+                                double* volume, double* avg_sigma, double* avg_F)
 {
   for (int e = 0; e < m->num_elem; e++) {
-    double x[24];
+    double x[24], vol_F;
     for (int n = 0; n < 8; n++) {
       int id = m->conn[8 * e + n];
       for (int k = 0; k < 3; k++) x[3 * n + k] = m->coords[3 * id + k] + u[3 * id + k];
     }
-    nsm_oracle_volume_average(x, sigma + 48 * (size_t)e, volume + e, avg + 6 * (size_t)e);
+    nsm_oracle_volume_average(x, 6, sigma + 48 * (size_t)e, volume + e, avg_sigma + 6 * (size_t)e);
+    nsm_oracle_volume_average(x, 9, F + 72 * (size_t)e, &vol_F, avg_F + 9 * (size_t)e);
   }
 }
 
@@ -524,8 +583,11 @@ nsm_oracle_lumped_mass(const nsm_oracle_model* m, double* mass)
   for (int n = 0; n < m->num_nodes; n++) mass[n] = 0.0;
   double X[24], me[8];
   for (int e = 0; e < m->num_elem; e++) {
+    int    model;
+    double rho, K, G;
+    material_of(m, e, &model, &rho, &K, &G);
     gather_element(m, e, m->coords, X);
-    element_lumped_mass(X, m->density, me);
+    element_lumped_mass(X, rho, me);
     for (int n = 0; n < 8; n++) mass[m->conn[8 * e + n]] += me[n];
   }
 }
@@ -560,19 +622,37 @@ characteristic_length(const double* c)
   return len;
 }
 
+/* BlockBase::ComputeCriticalTimeStep (src/nimble_block_base.cc:51-84) per
+ * block, the least over the blocks. */
 double
 nsm_oracle_critical_time_step(const nsm_oracle_model* m)
 {
-  const double sound_speed = sqrt(m->bulk_modulus / m->density);
-  double       dt          = DBL_MAX;
-  double       c[24];
+  double dt = DBL_MAX;
+  double c[24];
   for (int e = 0; e < m->num_elem; e++) {
+    int    model;
+    double rho, K, G;
+    material_of(m, e, &model, &rho, &K, &G);
+    const double sound_speed = sqrt(K / rho);
     gather_element(m, e, m->coords, c);
     for (int i = 0; i < 24; i++) c[i] = c[i] + 0.0; /* X + u with u = 0 at setup */
     double dte = characteristic_length(c) / sound_speed;
     if (dte < dt) dt = dte;
   }
   return dt;
+}
+
+/* Strain energy density of the elastic material, W = mu eps:eps +
+ * lambda/2 tr(eps)^2 with the strain of elastic_point (not in the
+ * reference; its stress is elastic_point's). */
+static double
+elastic_energy_density(const double* F, double K, double G)
+{
+  const double lambda = K - 2.0 * G / 3.0;
+  const double exx = F[0] - 1.0, eyy = F[1] - 1.0, ezz = F[2] - 1.0;
+  const double exy = 0.5 * (F[3] + F[6]), eyz = 0.5 * (F[4] + F[7]), ezx = 0.5 * (F[5] + F[8]);
+  const double tr = exx + eyy + ezz;
+  return G * (exx * exx + eyy * eyy + ezz * ezz + 2.0 * (exy * exy + eyz * eyz + ezx * ezx)) + 0.5 * lambda * tr * tr;
 }
 
 /* Strain energy density, evaluated from H = F - I without cancellation:
@@ -659,8 +739,11 @@ internal_force(work* w, const double* u, double* f_int, int num_threads)
     for (int i = 0; i < 24; i++) x[i] = X[i] + ue[i];
     double* F = &w->F[72 * (size_t)e];
     double* s = &w->sigma[48 * (size_t)e];
+    int    model;
+    double rho, K, G;
+    material_of(m, e, &model, &rho, &K, &G);
     nsm_oracle_deformation_gradients(X, x, F);
-    nsm_oracle_stress(8, F, m->bulk_modulus, m->shear_modulus, s);
+    nsm_oracle_stress_model(model, 8, F, K, G, s);
     nsm_oracle_nodal_forces(x, s, &w->fe[24 * (size_t)e]);
     for (int ip = 0; ip < 8; ip++) {
       double a[3][3], ai[3][3];
@@ -867,12 +950,16 @@ nsm_oracle_energies(const nsm_oracle* o, double* ke, double* ie)
   if (o->step > 0) {
     for (int e = 0; e < m->num_elem; e++) {
       double X[24];
+      int    model;
+      double rho, K, G;
+      material_of(m, e, &model, &rho, &K, &G);
       gather_element(m, e, m->coords, X);
       for (int ip = 0; ip < 8; ip++) {
-        double b[3][3], bi[3][3];
+        double        b[3][3], bi[3][3];
+        const double* Fp = &o->w.F[72 * (size_t)e + 9 * ip];
         jacobian(X, ip, b);
-        e_int += invert3x3(b, bi) *
-                 nsm_oracle_energy_density(&o->w.F[72 * (size_t)e + 9 * ip], m->bulk_modulus, m->shear_modulus);
+        e_int += invert3x3(b, bi) * (model == NSM_ORACLE_ELASTIC ? elastic_energy_density(Fp, K, G)
+                                                                 : nsm_oracle_energy_density(Fp, K, G));
       }
     }
   }

@@ -36,7 +36,22 @@ typedef struct nsm_oracle_model {
   const double* bc_value;     /* [num_bcs] */
   const int*    bc_ptr;       /* [num_bcs+1] offsets into bc_nodes */
   const int*    bc_nodes;
+  /* Material model of the single material (NSM_ORACLE_NEOHOOKEAN /
+   * NSM_ORACLE_ELASTIC, the names of src/nimble_material_factory.cc:57-70).
+   * With num_blocks > 1 each element takes the material of its block
+   * (elem_block [E], elements ordered by block) and the single-material
+   * fields above are unused. */
+  int           material_model;
+  int           num_blocks;
+  const int*    elem_block;    /* [E] */
+  const int*    block_model;   /* [num_blocks] */
+  const double* block_density; /* [num_blocks] */
+  const double* block_bulk;    /* [num_blocks] */
+  const double* block_shear;   /* [num_blocks] */
 } nsm_oracle_model;
+
+#define NSM_ORACLE_NEOHOOKEAN 0
+#define NSM_ORACLE_ELASTIC 1
 
 /* Results of a run.  Every pointer may be NULL. */
 typedef struct nsm_oracle_result {
@@ -64,6 +79,12 @@ void nsm_oracle_deformation_gradients(const double* X, const double* x, double* 
 /* Neo-Hookean Cauchy stress of n points (src/nimble_material.cc:226-310). */
 void nsm_oracle_stress(int n, const double* F, double bulk_modulus, double shear_modulus, double* sigma);
 
+/* Cauchy stress of n points of the given material model (NSM_ORACLE_*):
+ * neo-Hookean as above, or ElasticMaterial::GetStress
+ * (src/nimble_material.cc:67-126). */
+void nsm_oracle_stress_model(
+    int model, int n, const double* F, double bulk_modulus, double shear_modulus, double* sigma);
+
 /* Nodal forces of one element (src/nimble_element.h:540-625 through
  * src/nimble_element.cc:457-472).  x [8][3] current coords, sigma [8][6]. */
 void nsm_oracle_nodal_forces(const double* x, const double* sigma, double* f);
@@ -72,10 +93,10 @@ void nsm_oracle_nodal_forces(const double* x, const double* sigma, double* f);
 void nsm_oracle_element(
     const double* X, const double* u, double bulk_modulus, double shear_modulus, double* F, double* sigma, double* f);
 
-/* Volume average of one element's point stresses (src/nimble_element.cc:262-282,
- * src/nimble_element.h:343-392): x [8][3] current coordinates, q [8][6];
- * volume and avg [6] out. */
-void nsm_oracle_volume_average(const double* x, const double* q, double* volume, double* avg);
+/* Volume average of nq point quantities of one element (src/nimble_element.cc:262-282,
+ * src/nimble_element.h:343-392): x [8][3] current coordinates, q [8][nq]
+ * (nq <= 32); volume and avg [nq] out. */
+void nsm_oracle_volume_average(const double* x, int nq, const double* q, double* volume, double* avg);
 
 /* Lumped mass (src/nimble_model_data.cc:495-530, src/nimble_block.cc:110-146,
  * src/nimble_element.cc:173-193) and critical time step
@@ -84,9 +105,9 @@ void   nsm_oracle_lumped_mass(const nsm_oracle_model* m, double* mass);
 double nsm_oracle_critical_time_step(const nsm_oracle_model* m);
 
 /* Derived element output over a model (src/nimble_block.cc:438-497): u [N][3],
- * sigma [E][8][6] -> volume [E], avg [E][6]. */
-void nsm_oracle_derived_element_data(const nsm_oracle_model* m, const double* u, const double* sigma, double* volume,
-                                     double* avg);
+ * sigma [E][8][6], F [E][8][9] -> volume [E], avg_sigma [E][6], avg_F [E][9]. */
+void nsm_oracle_derived_element_data(const nsm_oracle_model* m, const double* u, const double* sigma, const double* F,
+                                     double* volume, double* avg_sigma, double* avg_F);
 
 /* Strain energy density W(F) whose Cauchy stress is the reference's
  * neo-Hookean stress: W = K/4 (J^2-1) - K/2 ln J + G/2 (J^{-2/3} tr(F F^T) - 3).

@@ -50,6 +50,8 @@ class _Model(C.Structure):
         ("density", C.c_double), ("bulk_modulus", C.c_double), ("shear_modulus", C.c_double),
         ("num_bcs", C.c_int), ("bc_kind", _ip), ("bc_component", _ip), ("bc_value", _dp),
         ("bc_ptr", _ip), ("bc_nodes", _ip),
+        ("material_model", C.c_int), ("num_blocks", C.c_int), ("elem_block", _ip), ("block_model", _ip),
+        ("block_density", _dp), ("block_bulk", _dp), ("block_shear", _dp),
     ]
 
 
@@ -96,8 +98,8 @@ def port():
         lib.nsm_oracle_set_state.argtypes = [C.c_void_p, _dp, _dp, _dp]
         lib.nsm_oracle_energies.argtypes = [C.c_void_p, _dp, _dp]
         lib.nsm_oracle_stress_exact.argtypes = [C.POINTER(_Model), _dp, C.c_int, _ip, _dp]
-        lib.nsm_oracle_volume_average.argtypes = [_dp, _dp, _dp, _dp]
-        lib.nsm_oracle_derived_element_data.argtypes = [C.POINTER(_Model), _dp, _dp, _dp, _dp]
+        lib.nsm_oracle_volume_average.argtypes = [_dp, C.c_int, _dp, _dp, _dp]
+        lib.nsm_oracle_derived_element_data.argtypes = [C.POINTER(_Model), _dp, _dp, _dp, _dp, _dp, _dp]
         _port = lib
     return _port
 
@@ -115,9 +117,12 @@ def ref():
         lib.nimref_run.argtypes = [C.c_int, _dp, C.c_int, _ip, C.c_int, _ip, _ip, C.c_char_p, C.c_char_p,
                                    C.c_char_p, C.c_double, C.c_int, C.c_int, _dp,
                                    _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp]
+        lib.nimref_run_blocks.argtypes = [C.c_int, _dp, C.c_int, _ip, C.c_int, _ip, C.c_char_p, C.c_int, _ip, _ip,
+                                          C.c_char_p, C.c_char_p, C.c_double, C.c_int, C.c_int, _dp, C.c_int,
+                                          _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _ip]
         lib.nimref_element.argtypes = [_dp, _dp, C.c_double, C.c_double, C.c_double, _dp, _dp, _dp]
         lib.nimref_stress.argtypes = [C.c_int, _dp, C.c_double, C.c_double, _dp]
-        lib.nimref_volume_average.argtypes = [_dp, _dp, _dp, _dp]
+        lib.nimref_volume_average.argtypes = [_dp, C.c_int, _dp, _dp, _dp]
         lib.nimref_last_error.restype = C.c_char_p
         _ref = lib
     return _ref
@@ -127,10 +132,18 @@ def _model(problem, keep):
     kinds, comps, vals, ptr, nodes = problem.bc_arrays()
     coords = np.ascontiguousarray(problem.coords, dtype=np.float64)
     conn = np.ascontiguousarray(problem.conn, dtype=np.int32)
-    keep.extend([kinds, comps, vals, ptr, nodes, coords, conn])
-    return _Model(problem.num_nodes, problem.num_elem, _d(coords), _i(conn), problem.density,
-                  problem.bulk_modulus, problem.shear_modulus, len(kinds), _i(kinds), _i(comps), _d(vals),
-                  _i(ptr), _i(nodes))
+    mats = problem.materials()
+    bm = np.array([mt.MODELS[mt.model] for mt in mats], np.int32)
+    bd = np.array([mt.density for mt in mats])
+    bk = np.array([mt.bulk_modulus for mt in mats])
+    bs = np.array([mt.shear_modulus for mt in mats])
+    eb = (np.ascontiguousarray(problem.elem_block, dtype=np.int32) if len(mats) > 1
+          else np.zeros(problem.num_elem, np.int32))
+    keep.extend([kinds, comps, vals, ptr, nodes, coords, conn, bm, bd, bk, bs, eb])
+    m0 = mats[0]
+    return _Model(problem.num_nodes, problem.num_elem, _d(coords), _i(conn), m0.density,
+                  m0.bulk_modulus, m0.shear_modulus, len(kinds), _i(kinds), _i(comps), _d(vals),
+                  _i(ptr), _i(nodes), int(bm[0]), len(mats), _i(eb), _i(bm), _d(bd), _d(bk), _d(bs))
 
 
 def _outputs(problem, with_ip):
@@ -216,10 +229,12 @@ def continue_port(problem, u, v, a, t0, dt, num_steps, threads):
     return secs.value
 
 
-def run_ref(problem, final_time, num_steps, output_frequency=0, with_ip=True):
-    """Runs the reference itself (oracle/_ref); same outputs as run_port."""
+def run_ref_outputs(problem, final_time, num_steps, output_frequency=0, with_ip=True):
+    """Runs the reference itself (oracle/_ref) and returns its state after
+    every output step of the schedule (after the last step only when
+    output_frequency is 0): a list of dicts like run_port's, F and sigma being
+    the element data the reference stored in that step."""
     lib = ref()
-    kinds, comps, vals, ptr, nodes = problem.bc_arrays()
     names = list(problem.node_sets.keys())
     ns_ptr = np.zeros(len(names) + 1, np.int32)
     parts = []
@@ -229,22 +244,39 @@ def run_ref(problem, final_time, num_steps, output_frequency=0, with_ip=True):
         ns_ptr[s + 1] = ns_ptr[s] + len(ids)
     ns_nodes = np.concatenate(parts).astype(np.int32) if parts else np.zeros(0, np.int32)
     bcs = "\n".join(bc.line() for bc in problem.bcs)
-    out = _outputs(problem, with_ip)
+    N, E = problem.num_nodes, problem.num_elem
+    of = int(output_frequency)
+    T = 1 if of == 0 else (int(num_steps) + of - 1) // of + 1
+    out = {k: np.zeros((T, N, 3)) for k in ("u", "v", "a", "f_int")}
+    if with_ip:
+        out["F"], out["sigma"] = np.zeros((T, E, 8, 9)), np.zeros((T, E, 8, 6))
+    mass = np.zeros(N)
     coords = np.ascontiguousarray(problem.coords, dtype=np.float64)
     conn = np.ascontiguousarray(problem.conn, dtype=np.int32)
+    mats = problem.materials()
+    eb = np.ascontiguousarray(problem.elem_block, dtype=np.int32) if len(mats) > 1 else None
     v0 = None if problem.v_init is None else np.ascontiguousarray(problem.v_init, dtype=np.float64)
-    dt = C.c_double(0.0)
-    secs = C.c_double(0.0)
-    rc = lib.nimref_run(problem.num_nodes, _d(coords), problem.num_elem, _i(conn), len(names), _i(ns_ptr),
-                        _i(ns_nodes), "\n".join(names).encode(), problem.material_line().encode(),
-                        bcs.encode(), float(final_time), int(num_steps), int(output_frequency), _d(v0),
-                        _d(out["u"]), _d(out["v"]), _d(out["a"]), _d(out["f_int"]), _d(out.get("F")),
-                        _d(out.get("sigma")), _d(out["mass"]), C.cast(C.pointer(dt), _dp),
-                        C.cast(C.pointer(secs), _dp))
+    dt, secs, n = C.c_double(0.0), C.c_double(0.0), C.c_int(0)
+    rc = lib.nimref_run_blocks(N, _d(coords), E, _i(conn), len(mats), _i(eb),
+                               "\n".join(mt.line() for mt in mats).encode(), len(names), _i(ns_ptr), _i(ns_nodes),
+                               "\n".join(names).encode(), bcs.encode(), float(final_time), int(num_steps), of,
+                               _d(v0), T, _d(out["u"]), _d(out["v"]), _d(out["a"]), _d(out["f_int"]),
+                               _d(out.get("F")), _d(out.get("sigma")), _d(mass), C.cast(C.pointer(dt), _dp),
+                               C.cast(C.pointer(secs), _dp), C.byref(n))
     if rc != 0:
         raise RuntimeError("reference run failed: " + lib.nimref_last_error().decode())
-    out.update(dt_crit=dt.value, loop_seconds=secs.value)
-    return out
+    states = []
+    for t in range(n.value):
+        st = {k: v[t] for k, v in out.items()}
+        st.update(mass=mass, dt_crit=dt.value, loop_seconds=secs.value)
+        states.append(st)
+    return states
+
+
+def run_ref(problem, final_time, num_steps, output_frequency=0, with_ip=True):
+    """Runs the reference itself (oracle/_ref); same outputs as run_port (the
+    state after the last step)."""
+    return run_ref_outputs(problem, final_time, num_steps, output_frequency, with_ip)[-1]
 
 
 def element(X, u, K, G, which="port"):
@@ -283,30 +315,35 @@ def stress_exact(problem, u, elems):
     return out
 
 
-def volume_average(x_cur, sigma, which="port"):
-    """One element's volume and volume-averaged stress (x_cur [8,3], sigma
-    [8,6]) -> (volume, avg [6]), HexElement::ComputeVolumeAverage."""
+def volume_average(x_cur, q, which="port"):
+    """One element's volume and volume average of point quantities q
+    ([8, nq]) at current coordinates x_cur ([8, 3]) -> (volume, avg [nq]),
+    HexElement::ComputeVolumeAverage."""
     x = np.ascontiguousarray(x_cur, dtype=np.float64)
-    q = np.ascontiguousarray(sigma, dtype=np.float64)
-    vol, avg = C.c_double(0.0), np.zeros(6)
+    q = np.ascontiguousarray(q, dtype=np.float64).reshape(8, -1)
+    nq = q.shape[1]
+    vol, avg = C.c_double(0.0), np.zeros(nq)
     if which == "port":
-        port().nsm_oracle_volume_average(_d(x), _d(q), C.cast(C.pointer(vol), _dp), _d(avg))
+        port().nsm_oracle_volume_average(_d(x), nq, _d(q), C.cast(C.pointer(vol), _dp), _d(avg))
     else:
-        if ref().nimref_volume_average(_d(x), _d(q), C.cast(C.pointer(vol), _dp), _d(avg)) != 0:
+        if ref().nimref_volume_average(_d(x), nq, _d(q), C.cast(C.pointer(vol), _dp), _d(avg)) != 0:
             raise RuntimeError(ref().nimref_last_error().decode())
     return vol.value, avg
 
 
-def derived_element_data(problem, u, sigma):
-    """Element volume [E] and volume-averaged stress [E,6] of displacement u
-    ([N,3]) and point stresses sigma ([E,8,6]), Block::ComputeDerivedElementData."""
+def derived_element_data(problem, u, sigma, F):
+    """Element volume [E] and volume-averaged stress [E,6] and deformation
+    gradient [E,9] of displacement u ([N,3]) and point data sigma ([E,8,6]),
+    F ([E,8,9]), Block::ComputeDerivedElementData."""
     keep = []
     m = _model(problem, keep)
     u = np.ascontiguousarray(u, dtype=np.float64)
     q = np.ascontiguousarray(sigma, dtype=np.float64)
-    vol, avg = np.zeros(problem.num_elem), np.zeros((problem.num_elem, 6))
-    port().nsm_oracle_derived_element_data(C.byref(m), _d(u), _d(q), _d(vol), _d(avg))
-    return vol, avg
+    f = np.ascontiguousarray(F, dtype=np.float64)
+    E = problem.num_elem
+    vol, avg, avg_F = np.zeros(E), np.zeros((E, 6)), np.zeros((E, 9))
+    port().nsm_oracle_derived_element_data(C.byref(m), _d(u), _d(q), _d(f), _d(vol), _d(avg), _d(avg_F))
+    return vol, avg, avg_F
 
 
 def shape_tables():

@@ -36,7 +36,9 @@ namespace {
 
 // Fills the protected members of the reference's mesh class
 // (src/nimble_genesis_mesh.h:328-354) directly, as ReadTextFile does
-// (src/nimble_genesis_mesh.cc:318-427), but from memory: one block with id 1.
+// (src/nimble_genesis_mesh.cc:318-427), but from memory: blocks with ids
+// 1..num_blocks (elem_block [E] 0-based block of each element, or null for
+// one block).
 class HarnessMesh : public nimble::GenesisMesh
 {
  public:
@@ -49,7 +51,9 @@ class HarnessMesh : public nimble::GenesisMesh
       int                             num_node_sets,
       const int*                      ns_ptr,
       const int*                      ns_nodes,
-      const std::vector<std::string>& ns_names)
+      const std::vector<std::string>& ns_names,
+      int                             num_blocks = 1,
+      const int*                      elem_block = nullptr)
   {
     file_name_ = "in_memory";
     dim_       = 3;
@@ -65,13 +69,22 @@ class HarnessMesh : public nimble::GenesisMesh
     }
     elem_global_id_.resize(num_elem);
     for (int e = 0; e < num_elem; e++) elem_global_id_[e] = e;
-    block_ids_                   = {1};
-    all_block_ids_               = {1};
-    block_names_[1]              = "block_1";
-    all_block_names_[1]          = "block_1";
-    block_elem_global_ids_[1]    = elem_global_id_;
-    block_num_nodes_per_elem_[1] = 8;
-    block_elem_connectivity_[1]  = std::vector<int>(conn, conn + 8 * static_cast<size_t>(num_elem));
+    for (int b = 0; b < num_blocks; b++) {
+      const int id = b + 1;
+      block_ids_.push_back(id);
+      all_block_ids_.push_back(id);
+      block_names_[id]              = "block_" + std::to_string(id);
+      all_block_names_[id]          = block_names_[id];
+      block_num_nodes_per_elem_[id] = 8;
+      block_elem_global_ids_[id]    = std::vector<int>();
+      block_elem_connectivity_[id]  = std::vector<int>();
+    }
+    for (int e = 0; e < num_elem; e++) {
+      const int id = (elem_block ? elem_block[e] : 0) + 1;
+      block_elem_global_ids_[id].push_back(e);
+      block_elem_connectivity_[id].insert(block_elem_connectivity_[id].end(), conn + 8 * static_cast<size_t>(e),
+                                          conn + 8 * static_cast<size_t>(e) + 8);
+    }
     for (int s = 0; s < num_node_sets; s++) {
       int id = s + 1;
       node_set_ids_.push_back(id);
@@ -147,31 +160,43 @@ nimref_last_error()
 
 /* Runs `num_steps` explicit steps of the reference on the given mesh.
  *
- * xyz[3N], conn[8E] (0-based, reference corner order), node sets in CSR form
- * (ns_ptr[num_node_sets+1], ns_nodes) with '\n'-separated names, the material
- * line as in an input deck ("neohookean density .. bulk_modulus .. shear_modulus .."),
+ * xyz[3N], conn[8E] (0-based, reference corner order); elem_block [E]
+ * (0-based block of each element, non-decreasing; null: one block) with one
+ * '\n'-separated material line per block as in an input deck ("<model>
+ * density .. bulk_modulus .. shear_modulus .."); node sets in CSR form
+ * (ns_ptr[num_node_sets+1], ns_nodes) with '\n'-separated names;
  * '\n'-separated boundary-condition lines.  v_init (nullable, [N][3]) is
  * written into the velocity after ApplyInitialConditions and before
- * ApplyKinematicConditions(0,0).  Outputs: u, v, a, f_int [N][3]; F [E][8][9]
- * and sigma [E][8][6] in the reference component order (nullable); lumped
- * mass [N]; critical time step; wall seconds of the step loop.
- * Returns 0, or -1 with nimref_last_error() set. */
+ * ApplyKinematicConditions(0,0).
+ *
+ * The state is recorded after every output step of the schedule (the steps
+ * the reference writes, src/integrators/explicit_time_integrator.cc:192-194;
+ * only the last step when output_frequency is 0), at most max_outputs of
+ * them, into out_* arrays laid out [output][...]: u, v, a, f_int [N][3]; F
+ * [E][8][9] and sigma [E][8][6] in the reference component order, copied
+ * from the element data the reference stored in that step (nullable).
+ * Also the lumped mass [N], the critical time step, the wall seconds of the
+ * step loop and the number of recorded outputs.  Returns 0, or -1 with
+ * nimref_last_error() set. */
 int
-nimref_run(
+nimref_run_blocks(
     int           num_nodes,
     const double* xyz,
     int           num_elem,
     const int*    conn,
+    int           num_blocks,
+    const int*    elem_block,
+    const char*   materials,
     int           num_node_sets,
     const int*    ns_ptr,
     const int*    ns_nodes,
     const char*   ns_names,
-    const char*   material,
     const char*   bcs,
     double        final_time,
     int           num_steps,
     int           output_frequency,
     const double* v_init,
+    int           max_outputs,
     double*       out_u,
     double*       out_v,
     double*       out_a,
@@ -180,11 +205,13 @@ nimref_run(
     double*       out_sigma,
     double*       out_mass,
     double*       out_dt_crit,
-    double*       out_loop_seconds)
+    double*       out_loop_seconds,
+    int*          out_num_outputs)
 {
   try {
     HarnessMesh mesh;
-    mesh.Fill(num_nodes, xyz, num_elem, conn, num_node_sets, ns_ptr, ns_nodes, SplitLines(ns_names));
+    mesh.Fill(num_nodes, xyz, num_elem, conn, num_node_sets, ns_ptr, ns_nodes, SplitLines(ns_names), num_blocks,
+              elem_block);
 
     HarnessParser parser;
     {
@@ -196,8 +223,13 @@ nimref_run(
     }
     parser.Set("number of load steps", std::to_string(num_steps));
     parser.Set("output frequency", std::to_string(output_frequency));
-    parser.Set("material parameters", std::string("material_1 ") + material);
-    parser.Set("element block", "block_1 material_1");
+    auto mat_lines = SplitLines(materials);
+    if (static_cast<int>(mat_lines.size()) != num_blocks) throw std::invalid_argument("one material line per block");
+    for (int b = 0; b < num_blocks; b++) {
+      const std::string id = std::to_string(b + 1);
+      parser.Set("material parameters", "material_" + id + " " + mat_lines[b]);
+      parser.Set("element block", "block_" + id + " material_" + id);
+    }
     parser.Set("output fields", "displacement");
     for (auto const& bc : SplitLines(bcs)) parser.Set("boundary condition", bc);
 
@@ -205,6 +237,7 @@ nimref_run(
     auto                model_data_ptr = data_manager.GetModelData();
     auto&               model_data     = *model_data_ptr;
     model_data.InitializeBlocks(data_manager, std::make_shared<nimble::MaterialFactory>());
+    auto& host_model = *std::dynamic_pointer_cast<nimble::ModelData>(model_data_ptr);
 
     // ---- src/integrators/explicit_time_integrator.cc:104-147 ----
     auto displacement   = model_data.GetVectorNodeData("displacement");
@@ -231,6 +264,41 @@ nimref_run(
         for (int k = 0; k < 3; k++) velocity(i, k) = v_init[3 * i + k];
     }
     model_data.ApplyKinematicConditions(data_manager, 0.0, 0.0);
+
+    // The state after a step: nodal fields, and F and sigma of every point
+    // from the element data stored in the step (after UpdateStates the
+    // newest values are the "n" data; per element 8 points x [F(9), sigma(6)],
+    // src/nimble_block.cc:85-108).
+    int  recorded = 0;
+    auto record   = [&]() {
+      if (recorded >= max_outputs) return;
+      const size_t o = static_cast<size_t>(recorded);
+      for (int i = 0; i < num_nodes; i++) {
+        for (int k = 0; k < 3; k++) {
+          const size_t j = o * 3 * num_nodes + 3 * i + k;
+          if (out_u) out_u[j] = displacement(i, k);
+          if (out_v) out_v[j] = velocity(i, k);
+          if (out_a) out_a[j] = acceleration(i, k);
+          if (out_fint) out_fint[j] = internal_force(i, k);
+        }
+      }
+      if (out_F || out_sigma) {
+        for (int b = 0; b < num_blocks; b++) {
+          const std::vector<double>& data = host_model.GetElementDataOld(b + 1);
+          const std::vector<int>&    ids  = mesh.GetElementGlobalIdsInBlock(b + 1);
+          const size_t               per  = data.size() / (ids.empty() ? 1 : ids.size()) / 8;
+          for (size_t le = 0; le < ids.size(); le++) {
+            const size_t e = static_cast<size_t>(ids[le]);
+            for (int ip = 0; ip < 8; ip++) {
+              const double* src = &data[(le * 8 + ip) * per];
+              if (out_F) std::memcpy(out_F + o * 72 * num_elem + 72 * e + 9 * ip, src, 9 * sizeof(double));
+              if (out_sigma) std::memcpy(out_sigma + o * 48 * num_elem + 48 * e + 6 * ip, src + 9, 6 * sizeof(double));
+            }
+          }
+        }
+      }
+      recorded++;
+    };
 
     auto t0 = std::chrono::steady_clock::now();
     // ---- src/integrators/explicit_time_integrator.cc:177-278 ----
@@ -267,49 +335,76 @@ nimref_run(
 
       if (is_output_step) { model_data.ApplyKinematicConditions(data_manager, time_current, time_previous); }
       model_data.UpdateStates(data_manager);
+      if (is_output_step || (output_frequency == 0 && step == num_load_steps - 1)) record();
     }
     auto t1 = std::chrono::steady_clock::now();
 
     if (out_loop_seconds) *out_loop_seconds = std::chrono::duration<double>(t1 - t0).count();
     if (out_dt_crit) *out_dt_crit = critical_time_step;
-    for (int i = 0; i < num_nodes; i++) {
-      for (int k = 0; k < 3; k++) {
-        if (out_u) out_u[3 * i + k] = displacement(i, k);
-        if (out_v) out_v[3 * i + k] = velocity(i, k);
-        if (out_a) out_a[3 * i + k] = acceleration(i, k);
-        if (out_fint) out_fint[3 * i + k] = internal_force(i, k);
-      }
-      if (out_mass) out_mass[i] = lumped_mass(i);
-    }
-
-    // Per-integration-point F and sigma of the last internal-force evaluation:
-    // re-evaluated from the final displacement with the reference's own
-    // element and material (the same calls the block functor makes,
-    // src/nimble_block.cc:309-352), which reproduces the stored values exactly.
-    if (out_F || out_sigma) {
-      nimble::HexElement element;
-      auto               block    = std::dynamic_pointer_cast<nimble::ModelData>(model_data_ptr)->GetBlocks().at(1);
-      auto               nh       = MakeNeohookean(block->GetDensity(), block->GetBulkModulus(), block->GetShearModulus());
-      double             ref_coord[24], cur_coord[24], F[72], sig[48];
-      for (int e = 0; e < num_elem; e++) {
-        for (int n = 0; n < 8; n++) {
-          int id = conn[8 * e + n];
-          for (int k = 0; k < 3; k++) {
-            ref_coord[3 * n + k] = xyz[3 * id + k];
-            cur_coord[3 * n + k] = xyz[3 * id + k] + displacement(id, k);
-          }
-        }
-        element.ComputeDeformationGradients(ref_coord, cur_coord, F);
-        nh.Stress(8, F, sig);
-        if (out_F) std::memcpy(out_F + 72 * static_cast<size_t>(e), F, sizeof(F));
-        if (out_sigma) std::memcpy(out_sigma + 48 * static_cast<size_t>(e), sig, sizeof(sig));
-      }
-    }
+    if (out_mass)
+      for (int i = 0; i < num_nodes; i++) out_mass[i] = lumped_mass(i);
+    if (out_num_outputs) *out_num_outputs = recorded;
     return 0;
   } catch (std::exception const& ex) {
     g_last_error = ex.what();
     return -1;
   }
+}
+
+/* One block of one material; the state after the last step only (see
+ * nimref_run_blocks).  material: "<model> density .. bulk_modulus .. shear_modulus ..". */
+int
+nimref_run(
+    int           num_nodes,
+    const double* xyz,
+    int           num_elem,
+    const int*    conn,
+    int           num_node_sets,
+    const int*    ns_ptr,
+    const int*    ns_nodes,
+    const char*   ns_names,
+    const char*   material,
+    const char*   bcs,
+    double        final_time,
+    int           num_steps,
+    int           output_frequency,
+    const double* v_init,
+    double*       out_u,
+    double*       out_v,
+    double*       out_a,
+    double*       out_fint,
+    double*       out_F,
+    double*       out_sigma,
+    double*       out_mass,
+    double*       out_dt_crit,
+    double*       out_loop_seconds)
+{
+  std::vector<double> u, v, a, f, F, S;
+  int                 n = 0;
+  const int           max_out =
+      output_frequency == 0 ? 1 : (num_steps + output_frequency - 1) / output_frequency + 1;
+  if (out_u) u.resize(static_cast<size_t>(max_out) * 3 * num_nodes);
+  if (out_v) v.resize(static_cast<size_t>(max_out) * 3 * num_nodes);
+  if (out_a) a.resize(static_cast<size_t>(max_out) * 3 * num_nodes);
+  if (out_fint) f.resize(static_cast<size_t>(max_out) * 3 * num_nodes);
+  if (out_F) F.resize(static_cast<size_t>(max_out) * 72 * num_elem);
+  if (out_sigma) S.resize(static_cast<size_t>(max_out) * 48 * num_elem);
+  auto p  = [](std::vector<double>& x) { return x.empty() ? nullptr : x.data(); };
+  int  rc = nimref_run_blocks(num_nodes, xyz, num_elem, conn, 1, nullptr, material, num_node_sets, ns_ptr, ns_nodes,
+                             ns_names, bcs, final_time, num_steps, output_frequency, v_init, max_out, p(u), p(v),
+                             p(a), p(f), p(F), p(S), out_mass, out_dt_crit, out_loop_seconds, &n);
+  if (rc != 0 || n == 0) return rc != 0 ? rc : -1;
+  const size_t last = static_cast<size_t>(n - 1);
+  auto         copy = [&](double* dst, std::vector<double>& src, size_t per) {
+    if (dst) std::memcpy(dst, src.data() + last * per, per * sizeof(double));
+  };
+  copy(out_u, u, 3 * static_cast<size_t>(num_nodes));
+  copy(out_v, v, 3 * static_cast<size_t>(num_nodes));
+  copy(out_a, a, 3 * static_cast<size_t>(num_nodes));
+  copy(out_fint, f, 3 * static_cast<size_t>(num_nodes));
+  copy(out_F, F, 72 * static_cast<size_t>(num_elem));
+  copy(out_sigma, S, 48 * static_cast<size_t>(num_elem));
+  return 0;
 }
 
 /* One element through the reference: deformation gradients, neo-Hookean
@@ -356,15 +451,15 @@ nimref_stress(int n, const double* F, double bulk_modulus, double shear_modulus,
   }
 }
 
-/* The reference's volume average of one element's point stresses,
+/* The reference's volume average of nq point quantities of one element,
  * HexElement::ComputeVolumeAverage (src/nimble_element.cc:262-282):
- * x_cur [8][3], sigma [8][6] -> volume, avg [6]. */
+ * x_cur [8][3], q [8][nq] -> volume, avg [nq]. */
 int
-nimref_volume_average(const double* x_cur, const double* sigma, double* volume, double* avg)
+nimref_volume_average(const double* x_cur, int nq, const double* q, double* volume, double* avg)
 {
   try {
     nimble::HexElement element;
-    element.ComputeVolumeAverage(x_cur, 6, sigma, *volume, avg);
+    element.ComputeVolumeAverage(x_cur, nq, q, *volume, avg);
     return 0;
   } catch (std::exception const& ex) {
     g_last_error = ex.what();

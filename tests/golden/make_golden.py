@@ -38,19 +38,25 @@ def _names(var):
 
 def read_exodus(path):
     """Mesh and results of an Exodus II (NetCDF-3) file: 0-based connectivity
-    of block 1, node sets named nodelist_<id> when unnamed (as
-    src/nimble_genesis_mesh.cc:160-172 does), nodal and element variables."""
+    of all element blocks in file order (their ids in "block_ids", the block
+    index of each element in "elem_block"), node sets named nodelist_<id> when
+    unnamed (as src/nimble_genesis_mesh.cc:160-172 does), nodal and element
+    variables (element variables concatenated over the blocks)."""
     d = scipy.io.netcdf_file(path, "r", mmap=False)
     v = d.variables
     coords = np.stack([v["coordx"][:], v["coordy"][:], v["coordz"][:]], axis=1).astype(np.float64)
-    conn = v["connect1"][:].astype(np.int32) - 1
+    nblk = len([k for k in v if re.fullmatch(r"connect\d+", k)])
+    conns = [v[f"connect{b + 1}"][:].astype(np.int32) - 1 for b in range(nblk)]
+    conn = np.concatenate(conns, axis=0)
+    elem_block = np.concatenate([np.full(len(c), b, np.int32) for b, c in enumerate(conns)])
+    block_ids = v["eb_prop1"][:].astype(np.int32) if "eb_prop1" in v else np.arange(1, nblk + 1, dtype=np.int32)
     ns = {}
     if "ns_prop1" in v:
         names = _names(v["ns_names"]) if "ns_names" in v else [""] * len(v["ns_prop1"][:])
         for k, sid in enumerate(v["ns_prop1"][:]):
             nm = names[k] or f"nodelist_{int(sid)}"
             ns[nm] = v[f"node_ns{k + 1}"][:].astype(np.int32) - 1
-    out = {"coords": coords, "conn": conn, "node_sets": ns}
+    out = {"coords": coords, "conn": conn, "node_sets": ns, "elem_block": elem_block, "block_ids": block_ids}
     if "time_whole" in v:
         out["times"] = v["time_whole"][:].astype(np.float64)
         if "name_nod_var" in v:
@@ -58,29 +64,36 @@ def read_exodus(path):
                 out["nod:" + nm] = v[f"vals_nod_var{k + 1}"][:].astype(np.float64)
         if "name_elem_var" in v:
             for k, nm in enumerate(_names(v["name_elem_var"])):
-                key = f"vals_elem_var{k + 1}eb1"
-                if key in v:
-                    out["elem:" + nm] = v[key][:].astype(np.float64)
+                keys = [f"vals_elem_var{k + 1}eb{b + 1}" for b in range(nblk)]
+                if all(key in v for key in keys):
+                    out["elem:" + nm] = np.concatenate([v[key][:].astype(np.float64) for key in keys], axis=1)
     d.close()
     return out
 
 
 def read_deck(path):
-    """Material parameters and boundary-condition lines of an input deck."""
-    mat, bcs, keys = None, [], {}
+    """Materials, element blocks and boundary-condition lines of an input deck:
+    (materials {name: {model, density, ...}}, blocks {block name: material
+    name}, bc lines, other keys)."""
+    mats, blocks, bcs, keys = {}, {}, [], {}
     for line in open(path):
         line = line.split("#")[0].strip()
         if ":" not in line:
             continue
         k, val = (s.strip() for s in line.split(":", 1))
         if k == "material parameters":
-            mat = val.split()
+            w = val.split()
+            prm = {w[i]: float(w[i + 1]) for i in range(2, len(w) - 1, 2)}
+            prm["model"] = w[1]
+            mats[w[0]] = prm
+        elif k == "element block":
+            w = val.split()
+            blocks[w[0]] = w[1]
         elif k == "boundary condition":
             bcs.append(val)
         else:
             keys[k] = val
-    params = {mat[i]: float(mat[i + 1]) for i in range(2, len(mat) - 1, 2)}
-    return params, bcs, keys
+    return mats, blocks, bcs, keys
 
 
 def read_exodiff(path):
@@ -103,16 +116,22 @@ def gold_fixture(name, deck_dir, deck, genesis, gold, exodiff):
     base = os.path.join(REF, "test", "dynamics", deck_dir)
     mesh = read_exodus(os.path.join(base, genesis))
     res = read_exodus(os.path.join(base, gold))
-    params, bc_lines, keys = read_deck(os.path.join(base, deck))
+    mats, blocks, bc_lines, keys = read_deck(os.path.join(base, deck))
+    # the material of each mesh block, in the mesh's block order
+    block_mats = [mats[blocks[f"block_{int(bid)}"]] for bid in mesh["block_ids"]]
+    params = block_mats[0]
     tol = read_exodiff(os.path.join(base, exodiff))
     assert np.array_equal(mesh["coords"], res["coords"]), "gold file nodes are in mesh order"
     T = len(res["times"])
     N, E = mesh["coords"].shape[0], mesh["conn"].shape[0]
     fx = {
         "coords": mesh["coords"], "conn": mesh["conn"], "times": res["times"],
-        "ns_names": np.array(list(mesh["node_sets"].keys())),
+        "ns_names": np.array(list(mesh["node_sets"].keys())), "material_model": params["model"],
         "density": params["density"], "bulk_modulus": params["bulk_modulus"],
         "shear_modulus": params["shear_modulus"], "bc_lines": np.array(bc_lines),
+        "elem_block": mesh["elem_block"],
+        "block_models": np.array([bm["model"] for bm in block_mats]),
+        "block_params": np.array([[bm["density"], bm["bulk_modulus"], bm["shear_modulus"]] for bm in block_mats]),
         "final_time": float(keys["final time"]), "num_steps": int(keys["number of load steps"]),
         "output_frequency": int(keys.get("output frequency", "1")),
     }
@@ -122,30 +141,35 @@ def gold_fixture(name, deck_dir, deck, genesis, gold, exodiff):
         if "nod:" + field + "_x" in res:
             fx["gold:" + field] = np.stack([res[f"nod:{field}_{c}"] for c in _VEC], axis=2)  # [T,N,3]
             fx["tol:" + field] = np.array([tol.get(f"{field}_{c}", 0.0) for c in _VEC])
-    F = np.zeros((T, E, 8, 9))
-    S = np.zeros((T, E, 8, 6))
-    tF = np.zeros((8, 9))
-    tS = np.zeros((8, 6))
-    for ip in range(8):
-        for c, nm in enumerate(_FULL):
-            key = f"ipt{ip + 1:02d}_deformation_gradient_{nm}"
-            F[:, :, ip, c] = res["elem:" + key]
-            tF[ip, c] = tol.get(key, 0.0)
-        for c, nm in enumerate(_SYM):
-            key = f"ipt{ip + 1:02d}_stress_{nm}"
-            S[:, :, ip, c] = res["elem:" + key]
-            tS[ip, c] = tol.get(key, 0.0)
-    fx["gold:F"], fx["gold:sigma"], fx["tol:F"], fx["tol:sigma"] = F, S, tF, tS
+    if "nod:lumped_mass" in res:
+        fx["gold:lumped_mass"], fx["tol:lumped_mass"] = res["nod:lumped_mass"], tol.get("lumped_mass", 0.0)
+    # per-point fields (ipt01..ipt08) where the deck writes them
+    for key, comps, shape in (("deformation_gradient", _FULL, 9), ("stress", _SYM, 6)):
+        if "elem:ipt01_" + key + "_xx" not in res:
+            continue
+        G, tG = np.zeros((T, E, 8, shape)), np.zeros((8, shape))
+        for ip in range(8):
+            for c, nm in enumerate(comps):
+                k = f"ipt{ip + 1:02d}_{key}_{nm}"
+                G[:, :, ip, c] = res["elem:" + k]
+                tG[ip, c] = tol.get(k, 0.0)
+        tag = "F" if key == "deformation_gradient" else "sigma"
+        fx["gold:" + tag], fx["tol:" + tag] = G, tG
+    # element fields without a point prefix are the volume averages
+    # (Block::ComputeDerivedElementData); "volume" is the element volume
+    for key, comps, tag in (("deformation_gradient", _FULL, "F_avg"), ("stress", _SYM, "sigma_avg")):
+        if "elem:" + key + "_xx" in res:
+            fx["gold:" + tag] = np.stack([res[f"elem:{key}_{c}"] for c in comps], axis=2)  # [T,E,k]
+            fx["tol:" + tag] = np.array([tol.get(f"{key}_{c}", 0.0) for c in comps])
+    if "elem:volume" in res:
+        fx["gold:volume"], fx["tol:volume"] = res["elem:volume"], tol.get("volume", 0.0)
     np.savez_compressed(os.path.join(HERE, f"gold_{name}.npz"), **fx)
     print("wrote", name, {k: np.shape(v) for k, v in fx.items() if k.startswith("gold")})
 
 
 def problem_from_fixture(fx) -> Problem:
-    names = [str(s) for s in fx["ns_names"]]
-    return Problem(coords=fx["coords"], conn=fx["conn"], node_sets={n: fx["ns:" + n] for n in names},
-                   density=float(fx["density"]), bulk_modulus=float(fx["bulk_modulus"]),
-                   shear_modulus=float(fx["shear_modulus"]),
-                   bcs=[BoundaryCondition.parse(str(b)) for b in fx["bc_lines"]])
+    from tests.goldens import gold_problem
+    return gold_problem(fx)
 
 
 def ref_cube_fixture(name, n, jitter, seed, steps, output_frequency, sample_elems=None):
@@ -211,12 +235,14 @@ def ref_derived_fixture(name="cube4_jitter"):
     them (reference coordinates + displacement, src/nimble_block.cc:477-483)."""
     fx = np.load(os.path.join(HERE, f"ref_{name}.npz"))
     p = cube_problem(int(fx["n"]), jitter=float(fx["jitter"]), seed=int(fx["seed"]))
-    vol, avg = np.zeros(p.num_elem), np.zeros((p.num_elem, 6))
+    vol, avg, avg_F = np.zeros(p.num_elem), np.zeros((p.num_elem, 6)), np.zeros((p.num_elem, 9))
     for e in range(p.num_elem):
         ids = p.conn[e]
         x = p.coords[ids] + fx["u"][ids]
         vol[e], avg[e] = O.volume_average(x, fx["sigma"][e], which="ref")
-    np.savez_compressed(os.path.join(HERE, f"ref_derived_{name}.npz"), volume=vol, stress=avg)
+        _, avg_F[e] = O.volume_average(x, fx["F"][e], which="ref")
+    np.savez_compressed(os.path.join(HERE, f"ref_derived_{name}.npz"), volume=vol, stress=avg,
+                        deformation_gradient=avg_F)
     print("wrote derived", name)
 
 
@@ -247,47 +273,62 @@ def ref_points_fixture():
     print("wrote points", Fs.shape)
 
 
+GOLD_DECKS = (
+    ("single_elem_native_neohookean", "single_elem_complex_displacement", "single_elem_native_neohookean.in",
+     "single_elem.g", "single_elem_native_neohookean.gold.e", "single_elem_native_neohookean.exodiff"),
+    ("wave_in_bar", "wave_in_bar", "wave_in_bar.in", "wave_in_bar.g", "wave_in_bar.gold.e", "wave_in_bar.exodiff"),
+    ("rigid_body_motion", "rigid_body_motion", "rigid_body_motion.in", "rigid_body_motion.g",
+     "rigid_body_motion.gold.e", "rigid_body_motion.exodiff"),
+    ("simple_deformation_modes", "simple_deformation_modes", "simple_deformation_modes.in",
+     "simple_deformation_modes.g", "simple_deformation_modes.gold.e", "simple_deformation_modes.exodiff"),
+    ("notched_plate_native_neohookean", "notched_plate_native_neohookean", "notched_plate_native_neohookean.in",
+     "notched_plate_native_neohookean.g", "notched_plate_native_neohookean.gold.e",
+     "notched_plate_native_neohookean.exodiff"),
+    ("notched_plate_native_hypoelastic", "notched_plate_native_hypoelastic", "notched_plate_native_hypoelastic.in",
+     "notched_plate_native_hypoelastic.g", "notched_plate_native_hypoelastic.gold.e",
+     "notched_plate_native_hypoelastic.exodiff"),
+    ("brick_with_fibers", "brick_with_fibers", "brick_with_fibers.in", "brick_with_fibers.g",
+     "brick_with_fibers.gold.e", "brick_with_fibers.exodiff"),
+)
+
+
+def _derived_ref(p, u, F, sigma):
+    """The reference's derived element output of one state."""
+    E = p.num_elem
+    vol, avg_s, avg_F = np.zeros(E), np.zeros((E, 6)), np.zeros((E, 9))
+    for e in range(E):
+        ids = p.conn[e]
+        x = p.coords[ids] + u[ids]
+        vol[e], avg_s[e] = O.volume_average(x, sigma[e], which="ref")
+        _, avg_F[e] = O.volume_average(x, F[e], which="ref")
+    return vol, avg_s, avg_F
+
+
 def ref_gold_rerun():
-    """The reference itself on the gold decks, every output time, bitwise."""
-    for name in ("single_elem_native_neohookean", "wave_in_bar"):
+    """The reference itself on the gold decks, every output time, bitwise,
+    with its derived element output (volume, volume-averaged F and sigma)."""
+    for name, *_ in GOLD_DECKS:
         fx = dict(np.load(os.path.join(HERE, f"gold_{name}.npz")))
         p = problem_from_fixture(fx)
         steps, of = int(fx["num_steps"]), int(fx["output_frequency"])
+        states = O.run_ref_outputs(p, float(fx["final_time"]), steps, of)
         out_steps = [s + 1 for s in range(steps) if of != 0 and (s % of == 0 or s == steps - 1)]
-        res = {"out_steps": np.array(out_steps)}
+        assert len(states) == len(out_steps)
+        res = {"out_steps": np.array(out_steps), "mass": states[0]["mass"]}
         for k in ("u", "v", "a", "f_int", "F", "sigma"):
-            res[k] = []
-        # Each output state is the end of a run truncated at that step with the
-        # same time step: final_time is scaled so dt_user is unchanged only when
-        # exact; the full schedule is rerun instead to keep dt identical.
-        for s_end in out_steps:
-            r = _ref_run_until(p, float(fx["final_time"]), steps, of, s_end)
-            for k in ("u", "v", "a", "f_int", "F", "sigma"):
-                res[k].append(r[k])
-        np.savez_compressed(os.path.join(HERE, f"ref_{name}.npz"), **{k: np.array(v) for k, v in res.items()})
+            res[k] = np.array([st[k] for st in states])
+        derived = [_derived_ref(p, st["u"], st["F"], st["sigma"]) for st in states]
+        res["volume"] = np.array([d[0] for d in derived])
+        res["sigma_avg"] = np.array([d[1] for d in derived])
+        res["F_avg"] = np.array([d[2] for d in derived])
+        np.savez_compressed(os.path.join(HERE, f"ref_{name}.npz"), **res)
         print("wrote ref rerun", name, out_steps)
-
-
-def _ref_run_until(p, final_time, steps, of, s_end):
-    """Reference run of the deck's schedule stopped after s_end steps.  The
-    harness runs whole schedules, so the schedule is rerun with num_steps =
-    s_end and final_time = s_end * dt_user; this keeps dt_user bitwise equal
-    when final_time/steps*s_end/s_end rounds back, which is checked."""
-    dt_user = final_time / steps
-    ft = dt_user * s_end
-    assert ft / s_end == dt_user, "truncated schedule would change the time step"
-    # Output steps of the truncated run must match the full run's up to s_end.
-    r = O.run_ref(p, ft, s_end, of)
-    return r
 
 
 if __name__ == "__main__":
     O.build(ref=True)
-    gold_fixture("single_elem_native_neohookean", "single_elem_complex_displacement",
-                 "single_elem_native_neohookean.in", "single_elem.g", "single_elem_native_neohookean.gold.e",
-                 "single_elem_native_neohookean.exodiff")
-    gold_fixture("wave_in_bar", "wave_in_bar", "wave_in_bar.in", "wave_in_bar.g", "wave_in_bar.gold.e",
-                 "wave_in_bar.exodiff")
+    for deck in GOLD_DECKS:
+        gold_fixture(*deck)
     ref_points_fixture()
     ref_cube_fixture("cube4_jitter", 4, 0.2, 7, 20, 0)
     ref_cube_fixture("cube16_cfg0", 16, 0.0, 0, 500, 500, sample_elems=64)

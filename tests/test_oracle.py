@@ -5,7 +5,7 @@ import pytest
 
 from nimblesm_gb300.mesh import cube_problem, critical_time_step
 from oracle import oracle as O
-from tests.goldens import exodiff_ok, gold_problem, load, output_steps
+from tests.goldens import GOLD_DECKS, exodiff_ok, gold_checks, gold_problem, load, output_steps
 
 
 @pytest.fixture(scope="module", autouse=True)
@@ -46,15 +46,17 @@ def test_cube_runs_match_reference_bitwise(name):
 
 
 def test_derived_element_data_matches_reference_bitwise():
-    """Element volume and volume-averaged stress (Block::ComputeDerivedElementData)
+    """Element volume, volume-averaged stress and deformation gradient
+    (Block::ComputeDerivedElementData)
     on the reference's final state of the 4^3 run, against the reference's own
     HexElement::ComputeVolumeAverage."""
     fx = load("ref_cube4_jitter")
     dx = load("ref_derived_cube4_jitter")
     p = cube_problem(int(fx["n"]), jitter=float(fx["jitter"]), seed=int(fx["seed"]))
-    vol, avg = O.derived_element_data(p, fx["u"], fx["sigma"])
+    vol, avg, avg_F = O.derived_element_data(p, fx["u"], fx["sigma"], fx["F"])
     assert np.array_equal(vol, dx["volume"])
     assert np.array_equal(avg, dx["stress"])
+    assert np.array_equal(avg_F, dx["deformation_gradient"])
     assert abs(vol.sum() - 1.0) < 1e-3  # the unit cube, slightly deformed
 
 
@@ -64,11 +66,12 @@ def test_numpy_critical_time_step_matches_oracle():
     assert critical_time_step(p) == O.PortRun(p).dt_crit
 
 
-@pytest.mark.parametrize("name", ["single_elem_native_neohookean", "wave_in_bar"])
+@pytest.mark.parametrize("name", GOLD_DECKS)
 def test_gold_files(name):
-    """The reference's regression decks against their gold files, at the
-    exodiff tolerances, at every output time; and bit for bit against the
-    reference run here on the same deck."""
+    """The reference's regression decks (neo-Hookean and elastic materials,
+    one and two element blocks) against their gold files, at the exodiff
+    tolerances, at every output time, including the derived element output;
+    and bit for bit against the reference run here on the same deck."""
     fx = load("gold_" + name)
     rf = load("ref_" + name)
     p = gold_problem(fx)
@@ -76,20 +79,19 @@ def test_gold_files(name):
     run = O.PortRun(p)
     run.begin(float(fx["final_time"]), steps, of)
     done = 0
-    for t_index, s_end in enumerate(output_steps(steps, of)):
+    for t, s_end in enumerate(output_steps(steps, of)):
         run.advance(s_end - done)
         done = s_end
         st = run.state()
-        assert np.isclose(st["time"], fx["times"][t_index + 1], rtol=1e-12, atol=0)
-        for field, key in (("displacement", "u"), ("velocity", "v"), ("acceleration", "a"),
-                           ("internal_force", "f_int")):
-            if "gold:" + field in fx:
-                assert exodiff_ok(st[key], fx["gold:" + field][t_index + 1], fx["tol:" + field]), field
-        assert exodiff_ok(st["F"], fx["gold:F"][t_index + 1], fx["tol:F"])
-        assert exodiff_ok(st["sigma"], fx["gold:sigma"][t_index + 1], fx["tol:sigma"])
+        assert np.isclose(st["time"], fx["times"][t + 1], rtol=1e-12, atol=0)
+        vol, sig_avg, F_avg = O.derived_element_data(p, st["u"], st["sigma"], st["F"])
+        gold_checks(fx, t, st, vol, sig_avg, F_avg)
         # the reference itself, same deck, same machine arithmetic
         for key in ("u", "v", "a", "f_int", "F", "sigma"):
-            assert np.array_equal(st[key], rf[key][t_index]), key
+            assert np.array_equal(st[key], rf[key][t]), key
+        assert np.array_equal(st["mass"], rf["mass"])
+        assert np.array_equal(vol, rf["volume"][t]) and np.array_equal(sig_avg, rf["sigma_avg"][t])
+        assert np.array_equal(F_avg, rf["F_avg"][t])
 
 
 def test_thread_count_does_not_change_results():

@@ -192,6 +192,30 @@ __device__ __forceinline__ void element_work(const ElementArgs& a, const int e)
   if (bad || !finite) atomicOr(a.status, (bad ? NSM_STATUS_BAD_JACOBIAN : 0) | (finite ? 0 : NSM_STATUS_NONFINITE));
 }
 
+// Point records before the first evaluation: F = I, sigma = 0, as the
+// reference initialises its element data.
+template <typename T>
+__global__ void k_ip_identity(int E, long ld_e, T* __restrict__ ip)
+{
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= E) return;
+  for (int p = 0; p < 8; p++) {
+    T* rec = ip + ((size_t)p * ld_e + e) * kIpRecord;
+#pragma unroll
+    for (int i = 0; i < 3; i++) rec[full_slot(i, i)] = T(1);
+  }
+}
+
+cudaError_t launch_ip_identity(int E, long ld_e, void* ip, int ip_is_float, cudaStream_t stream)
+{
+  if (E == 0) return cudaSuccess;
+  if (ip_is_float)
+    k_ip_identity<float><<<grid_for(E, 128), 128, 0, stream>>>(E, ld_e, (float*)ip);
+  else
+    k_ip_identity<double><<<grid_for(E, 128), 128, 0, stream>>>(E, ld_e, (double*)ip);
+  return cudaGetLastError();
+}
+
 int num_sms()
 {
   static int n = 0;

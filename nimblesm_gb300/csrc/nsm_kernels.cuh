@@ -91,6 +91,8 @@ struct ElementLaunch {
 cudaError_t launch_element_fp64(const ElementArgs& a, const ElementLaunch& l, cudaStream_t stream);
 cudaError_t launch_element_fp32(const ElementArgs& a, const ElementLaunch& l, cudaStream_t stream);
 int         num_sms();
+// F = I (sigma = 0) in every point record: the element data before the first step.
+cudaError_t launch_ip_identity(int E, long ld_e, void* ip, int ip_is_float, cudaStream_t stream);
 
 // Node kernel: the end of step s (gather f_int, a = f/m, v += half*a, output
 // BCs) fused with the start of step s+1 (v += half*a, BCs, u += delta*v, BCs).

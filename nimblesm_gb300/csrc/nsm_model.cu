@@ -452,6 +452,7 @@ int create_impl(int S, const nsm_mesh_desc* meshes, int num_mats, const nsm_mate
   NSM_CUDA_B(cudaMalloc(&m->d_ip, eb * nsm::kIpRecord * 8 * m->ld_e));
   NSM_CUDA_B(cudaMalloc(&m->d_fe, eb * 24 * m->ld_e));
   NSM_CUDA_B(cudaMemsetAsync(m->d_ip, 0, eb * nsm::kIpRecord * 8 * m->ld_e, m->stream));
+  NSM_CUDA_B(nsm::launch_ip_identity(E, m->ld_e, m->d_ip, m->precision == NSM_PRECISION_FP64 ? 0 : 1, m->stream));
   NSM_CUDA_B(cudaMemsetAsync(m->d_fe, 0, eb * 24 * m->ld_e, m->stream));
   if (m->precision == NSM_PRECISION_FP32_MIXED) {
     NSM_CUDA_B(cudaMalloc(&m->d_Xf, sizeof(float) * 3 * m->ld_n));

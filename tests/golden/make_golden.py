@@ -27,73 +27,24 @@ sys.path.insert(0, ROOT)
 
 from nimblesm_gb300.mesh import (CORNER_SIGNS, BoundaryCondition, Problem, cube_problem,  # noqa: E402
                                  critical_time_step)
+from nimblesm_gb300.deck import read_deck as parse_deck  # noqa: E402
+from nimblesm_gb300.deck import read_genesis  # noqa: E402
 from oracle import oracle as O  # noqa: E402
 
 REF = "/root/reference"
 
 
-def _names(var):
-    return [b"".join(r).strip(b"\x00").decode() for r in var[:]]
-
-
 def read_exodus(path):
-    """Mesh and results of an Exodus II (NetCDF-3) file: 0-based connectivity
-    of all element blocks in file order (their ids in "block_ids", the block
-    index of each element in "elem_block"), node sets named nodelist_<id> when
-    unnamed (as src/nimble_genesis_mesh.cc:160-172 does), nodal and element
-    variables (element variables concatenated over the blocks)."""
-    d = scipy.io.netcdf_file(path, "r", mmap=False)
-    v = d.variables
-    coords = np.stack([v["coordx"][:], v["coordy"][:], v["coordz"][:]], axis=1).astype(np.float64)
-    nblk = len([k for k in v if re.fullmatch(r"connect\d+", k)])
-    conns = [v[f"connect{b + 1}"][:].astype(np.int32) - 1 for b in range(nblk)]
-    conn = np.concatenate(conns, axis=0)
-    elem_block = np.concatenate([np.full(len(c), b, np.int32) for b, c in enumerate(conns)])
-    block_ids = v["eb_prop1"][:].astype(np.int32) if "eb_prop1" in v else np.arange(1, nblk + 1, dtype=np.int32)
-    ns = {}
-    if "ns_prop1" in v:
-        names = _names(v["ns_names"]) if "ns_names" in v else [""] * len(v["ns_prop1"][:])
-        for k, sid in enumerate(v["ns_prop1"][:]):
-            nm = names[k] or f"nodelist_{int(sid)}"
-            ns[nm] = v[f"node_ns{k + 1}"][:].astype(np.int32) - 1
-    out = {"coords": coords, "conn": conn, "node_sets": ns, "elem_block": elem_block, "block_ids": block_ids}
-    if "time_whole" in v:
-        out["times"] = v["time_whole"][:].astype(np.float64)
-        if "name_nod_var" in v:
-            for k, nm in enumerate(_names(v["name_nod_var"])):
-                out["nod:" + nm] = v[f"vals_nod_var{k + 1}"][:].astype(np.float64)
-        if "name_elem_var" in v:
-            for k, nm in enumerate(_names(v["name_elem_var"])):
-                keys = [f"vals_elem_var{k + 1}eb{b + 1}" for b in range(nblk)]
-                if all(key in v for key in keys):
-                    out["elem:" + nm] = np.concatenate([v[key][:].astype(np.float64) for key in keys], axis=1)
-    d.close()
-    return out
+    """Mesh and results of an Exodus II (NetCDF-3) file (the engine's own
+    reader, nimblesm_gb300.deck.read_genesis)."""
+    return read_genesis(path)
 
 
 def read_deck(path):
-    """Materials, element blocks and boundary-condition lines of an input deck:
-    (materials {name: {model, density, ...}}, blocks {block name: material
-    name}, bc lines, other keys)."""
-    mats, blocks, bcs, keys = {}, {}, [], {}
-    for line in open(path):
-        line = line.split("#")[0].strip()
-        if ":" not in line:
-            continue
-        k, val = (s.strip() for s in line.split(":", 1))
-        if k == "material parameters":
-            w = val.split()
-            prm = {w[i]: float(w[i + 1]) for i in range(2, len(w) - 1, 2)}
-            prm["model"] = w[1]
-            mats[w[0]] = prm
-        elif k == "element block":
-            w = val.split()
-            blocks[w[0]] = w[1]
-        elif k == "boundary condition":
-            bcs.append(val)
-        else:
-            keys[k] = val
-    return mats, blocks, bcs, keys
+    """(materials {name: params}, blocks {block: material}, bc lines, other
+    keys) of an input deck (the engine's own parser, nimblesm_gb300.deck)."""
+    d = parse_deck(path)
+    return d.materials, d.blocks, d.bcs, d.keys
 
 
 def read_exodiff(path):
@@ -129,7 +80,8 @@ def gold_fixture(name, deck_dir, deck, genesis, gold, exodiff):
         "ns_names": np.array(list(mesh["node_sets"].keys())), "material_model": params["model"],
         "density": params["density"], "bulk_modulus": params["bulk_modulus"],
         "shear_modulus": params["shear_modulus"], "bc_lines": np.array(bc_lines),
-        "elem_block": mesh["elem_block"],
+        "elem_block": mesh["elem_block"], "block_ids": mesh["block_ids"],
+        "output_fields": keys.get("output fields", ""),
         "block_models": np.array([bm["model"] for bm in block_mats]),
         "block_params": np.array([[bm["density"], bm["bulk_modulus"], bm["shear_modulus"]] for bm in block_mats]),
         "final_time": float(keys["final time"]), "num_steps": int(keys["number of load steps"]),

@@ -132,6 +132,24 @@ int nsm_create_ensemble(int num_samples, const nsm_mesh_desc* meshes, const nsm_
  * elem_block NULL is a single block of any material model. */
 int nsm_create_blocks(const nsm_mesh_desc* mesh, int num_blocks, const int* elem_block, const nsm_material* materials,
                       const nsm_options* options, nsm_model** out);
+
+/* The reference's UQ mode on one mesh (nimble_uq::ModelData,
+ * src/uq/nimble_uq_model_data.cc:145-248, with UqModel, src/uq/nimble_uq.cc):
+ * trajectory 0 is the nominal (blocks and materials as nsm_create_blocks);
+ * trajectories 1..num_exact evaluate the element forces with their own bulk
+ * and shear moduli exact_bulk / exact_shear [num_exact][num_blocks]
+ * (nimble_uq::Block::ComputeInternalForce, src/uq/nimble_uq_block.cc:57-164);
+ * the last num_approx trajectories have no element work, their force being
+ * the linear closure f = c_0 f_nominal + sum_k c_k f_exact_k with
+ * coefficients [num_approx][num_exact + 1] (UqModel::ApplyClosure,
+ * src/uq/nimble_uq.cc:327-345), and they use the nominal's lumped mass.  The
+ * trajectories are samples of an ensemble (nsm_ensemble_offsets): give every
+ * trajectory the velocity-type conditions and the nominal alone the
+ * prescribed displacements (src/nimble_boundary_condition_manager.h:137-206),
+ * and all of them the nominal's schedule (nsm_begin_ensemble). */
+int nsm_create_uq(const nsm_mesh_desc* mesh, int num_blocks, const int* elem_block, const nsm_material* nominal,
+                  int num_exact, const double* exact_bulk, const double* exact_shear, int num_approx,
+                  const double* coefficients, const nsm_options* options, nsm_model** out);
 int nsm_ensemble_offsets(nsm_model* model, int* node_offsets, int* elem_offsets); /* [S+1] each */
 int nsm_ensemble_time_steps(nsm_model* model, double* dt);                      /* [S] critical steps */
 /* Per-sample max |field component| over the listed (global) node ids, out [S]

@@ -34,6 +34,27 @@ __device__ __forceinline__ double axpy(double s, double x, double y)
   return kExact ? __dadd_rn(y, __dmul_rn(s, x)) : fma(s, x, y);
 }
 
+// The assembled element force of node n: element contributions in increasing
+// element order.
+template <typename TF, bool kExact>
+__device__ __forceinline__ void gather_force(const NodeArgs& a, int n, double f[3])
+{
+  const TF* fe    = reinterpret_cast<const TF*>(a.fe);
+  TF        fs[3] = {TF(0), TF(0), TF(0)};
+  for (int k = a.node_ptr[n]; k < a.node_ptr[n + 1]; k++) {
+    const int  ec = __ldg(&a.node_inc[k]);
+    const long e  = ec >> 3;
+    const int  c  = ec & 7;
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      const TF x = __ldg(&fe[e * 24 + c * 3 + i]);
+      fs[i]      = kExact ? TF(__dadd_rn(double(fs[i]), double(x))) : fs[i] + x;
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 3; i++) f[i] = double(fs[i]);
+}
+
 template <typename TF, bool kExact>
 __global__ void __launch_bounds__(256) k_node_update(NodeArgs a)
 {
@@ -50,19 +71,25 @@ __global__ void __launch_bounds__(256) k_node_update(NodeArgs a)
     // ModelData::ComputeInternalForce: zero, then element contributions in
     // increasing element order (src/nimble_model_data.cc:620-667,
     // src/nimble_block.cc:373-383).
-    const TF* fe    = reinterpret_cast<const TF*>(a.fe);
-    TF        fs[3] = {TF(0), TF(0), TF(0)};
-    for (int k = a.node_ptr[n]; k < a.node_ptr[n + 1]; k++) {
-      const int  ec = __ldg(&a.node_inc[k]);
-      const long e  = ec >> 3;
-      const int  c  = ec & 7;
+    double f[3];
+    if (a.closure && group >= a.closure_first) {
+      // UqModel::ApplyClosure (src/uq/nimble_uq.cc:327-345): f = f_0 c_0, then
+      // f += f_k c_k over the exact samples, from the same assembled forces
+      // the nominal and exact samples' own nodes compute
+      const int     local = n - a.node_off[group];
+      const double* c     = a.closure + (long)(group - a.closure_first) * (a.num_exact + 1);
+      double        fk[3];
+      gather_force<TF, kExact>(a, a.node_off[0] + local, fk);
 #pragma unroll
-      for (int i = 0; i < 3; i++) {
-        const TF x = __ldg(&fe[e * 24 + c * 3 + i]);
-        fs[i]      = kExact ? TF(__dadd_rn(double(fs[i]), double(x))) : fs[i] + x;
+      for (int i = 0; i < 3; i++) f[i] = kExact ? __dmul_rn(fk[i], c[0]) : fk[i] * c[0];
+      for (int k = 1; k <= a.num_exact; k++) {
+        gather_force<TF, kExact>(a, a.node_off[k] + local, fk);
+#pragma unroll
+        for (int i = 0; i < 3; i++) f[i] = kExact ? __dadd_rn(f[i], __dmul_rn(fk[i], c[k])) : fma(fk[i], c[k], f[i]);
       }
+    } else {
+      gather_force<TF, kExact>(a, n, f);
     }
-    double f[3] = {double(fs[0]), double(fs[1]), double(fs[2])};
 #pragma unroll
     for (int i = 0; i < 3; i++) a.f_int[i * ld + n] = f[i];
     if (a.gather_only) return;

@@ -118,6 +118,12 @@ struct NodeArgs {
   double*           a;
   double*           f_int;
   float*            uf;       // FP32 copy of u kept in step (FP32 form), or null
+  // UQ closure (samples of one mesh): samples closure_first.. have no
+  // elements; their force is c0 f_0 + sum_k c_k f_k over samples 0..num_exact
+  // at the same local node (closure [sample - closure_first][num_exact + 1]).
+  const double*     closure;  // or null
+  int               closure_first, num_exact;
+  const int*        node_off; // [num_groups + 1] first node of each sample
 };
 
 cudaError_t launch_node_update(const NodeArgs& a, cudaStream_t stream);

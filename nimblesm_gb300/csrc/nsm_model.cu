@@ -82,6 +82,9 @@ struct nsm_model {
   int*    d_elem_group = nullptr;  // [E] material of each element (more than one material)
   int*    d_node_group = nullptr;  // [N] sample of each node (S > 1)
   int*    d_elem_off = nullptr;    // [S+1]
+  int*    d_node_off = nullptr;    // [S+1] (UQ closure)
+  double* d_closure = nullptr;     // [num_approx][num_exact+1] (UQ closure), or null
+  int     closure_first = 0, num_exact = 0;
   nsm::GroupMaterial* d_mats = nullptr;  // [num_mats]
   std::vector<double> dt_group;    // per-sample critical time step
   nsm::ElementLaunch  elaunch{128, 0, 0};
@@ -123,7 +126,7 @@ void free_all(nsm_model* m)
                   m->d_f,    m->d_fext,     m->d_mass,     m->d_inv_mass, m->d_geo,    m->d_ip,    m->d_Xf,
                   m->d_uf,   m->d_fe,   m->d_status,   m->d_step_base, m->d_scratch, m->d_stage,  m->d_out,   m->d_bc_slot,
                   m->d_bcs,  m->d_ibc_slot, m->d_ibcs,     m->d_sched, m->d_group_out, m->d_elem_group,
-                  m->d_node_group, m->d_elem_off, m->d_mats, m->d_fallbacks};
+                  m->d_node_group, m->d_elem_off, m->d_mats, m->d_fallbacks, m->d_node_off, m->d_closure};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (auto& e : m->ev_elem) {
@@ -259,6 +262,10 @@ nsm::NodeArgs node_args(nsm_model* m, int k_post, int k_pre, int gather_only)
   a.a           = m->d_a;
   a.f_int       = m->d_f;
   a.uf          = m->d_uf;
+  a.closure       = m->d_closure;
+  a.closure_first = m->closure_first;
+  a.num_exact     = m->num_exact;
+  a.node_off      = m->d_node_off;
   return a;
 }
 
@@ -602,6 +609,65 @@ int nsm_create_blocks(const nsm_mesh_desc* mesh, int num_blocks, const int* elem
 {
   if (!mesh || num_blocks < 1 || (num_blocks > 1 && !elem_block)) return fail(NSM_ERR_INVALID_ARGUMENT, "null argument");
   return create_impl(1, mesh, num_blocks, materials, num_blocks > 1 ? elem_block : nullptr, options, out);
+}
+
+int nsm_create_uq(const nsm_mesh_desc* mesh, int num_blocks, const int* elem_block, const nsm_material* nominal,
+                  int num_exact, const double* exact_bulk, const double* exact_shear, int num_approx,
+                  const double* coefficients, const nsm_options* options, nsm_model** out)
+{
+  if (!mesh || !nominal || !out || num_blocks < 1 || num_exact < 0 || num_approx < 0 ||
+      (num_blocks > 1 && !elem_block) || (num_exact > 0 && (!exact_bulk || !exact_shear)) ||
+      (num_approx > 0 && !coefficients))
+    return fail(NSM_ERR_INVALID_ARGUMENT, "null argument");
+  const int S = 1 + num_exact + num_approx, B = num_blocks, full = 1 + num_exact;
+  // trajectories: the nominal, the exact samples (elements, own moduli), the
+  // approximate samples (nodes only, force from the closure)
+  std::vector<nsm_mesh_desc> meshes(S, *mesh);
+  for (int s = full; s < S; s++) meshes[s] = nsm_mesh_desc{mesh->num_nodes, 0, mesh->coords, nullptr};
+  std::vector<nsm_material> mats((size_t)full * B);
+  for (int k = 0; k < full; k++)
+    for (int b = 0; b < B; b++) {
+      nsm_material mt = nominal[b];
+      if (k > 0) {
+        mt.bulk_modulus  = exact_bulk[(size_t)(k - 1) * B + b];
+        mt.shear_modulus = exact_shear[(size_t)(k - 1) * B + b];
+      }
+      mats[(size_t)k * B + b] = mt;
+    }
+  std::vector<int> emat((size_t)full * mesh->num_elem);
+  for (int k = 0; k < full; k++)
+    for (int e = 0; e < mesh->num_elem; e++)
+      emat[(size_t)k * mesh->num_elem + e] = k * B + (B > 1 ? elem_block[e] : 0);
+  int rc = create_impl(S, meshes.data(), full * B, mats.data(), emat.data(), options, out);
+  if (rc != NSM_OK) return rc;
+  nsm_model* m = *out;
+  cudaError_t e = cudaSuccess;
+  if (num_approx > 0) {
+    // the approximate samples use the nominal's lumped mass (mass[i / 3],
+    // src/uq/nimble_uq_model_data.cc:218-234)
+    const size_t nb = sizeof(double) * mesh->num_nodes;
+    for (int s = full; s < S && e == cudaSuccess; s++) {
+      e = cudaMemcpyAsync(m->d_mass + m->node_off[s], m->d_mass, nb, cudaMemcpyDeviceToDevice, m->stream);
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(m->d_inv_mass + m->node_off[s], m->d_inv_mass, nb, cudaMemcpyDeviceToDevice, m->stream);
+    }
+    if (e == cudaSuccess) e = cudaMalloc(&m->d_closure, sizeof(double) * num_approx * (num_exact + 1));
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(m->d_closure, coefficients, sizeof(double) * num_approx * (num_exact + 1),
+                          cudaMemcpyHostToDevice, m->stream);
+    if (e == cudaSuccess) e = cudaMalloc(&m->d_node_off, sizeof(int) * (S + 1));
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(m->d_node_off, m->node_off.data(), sizeof(int) * (S + 1), cudaMemcpyHostToDevice, m->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(m->stream);
+    m->closure_first = full;
+    m->num_exact     = num_exact;
+  }
+  if (e != cudaSuccess) {
+    nsm_destroy(m);
+    *out = nullptr;
+    return cuda_fail(e, "nsm_create_uq");
+  }
+  return NSM_OK;
 }
 
 int nsm_ensemble_offsets(nsm_model* m, int* node_offsets, int* elem_offsets)

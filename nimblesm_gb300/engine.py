@@ -15,7 +15,7 @@ import os
 
 import numpy as np
 
-from .mesh import Problem
+from .mesh import BC_PRESCRIBED_DISPLACEMENT, Problem
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_lib", "libnimble_gb300.so")
@@ -65,6 +65,8 @@ SIGNATURES = {
     "nsm_create": (C.c_int, [C.POINTER(_Mesh), C.POINTER(_Material), C.POINTER(_Options), C.POINTER(_vp)]),
     "nsm_create_blocks": (C.c_int, [C.POINTER(_Mesh), C.c_int, _ip, C.POINTER(_AnyMaterial), C.POINTER(_Options),
                                     C.POINTER(_vp)]),
+    "nsm_create_uq": (C.c_int, [C.POINTER(_Mesh), C.c_int, _ip, C.POINTER(_AnyMaterial), C.c_int, _dp, _dp, C.c_int,
+                                _dp, C.POINTER(_Options), C.POINTER(_vp)]),
     "nsm_destroy": (C.c_int, [_vp]),
     "nsm_add_boundary_condition": (C.c_int, [_vp, C.c_int, C.c_int, C.c_double, _ip, C.c_int]),
     "nsm_compute_lumped_mass": (C.c_int, [_vp, _dp]),
@@ -438,6 +440,65 @@ class MLPClosure:
         fb = C.c_int()
         _check_mlp(library().nsm_mlp_predict(self._h, F.shape[0], _d(F), _d(s), C.byref(fb)))
         return s, fb.value
+
+
+class UqModel(Model):
+    """The reference's UQ mode on one mesh (nsm_create_uq) for a UqSpec:
+    trajectory 0 is the nominal, then the exact samples (element forces with
+    their own moduli), then the approximate samples (force from the linear
+    closure).  Every trajectory gets the velocity-type conditions, the nominal
+    alone the prescribed displacements, all of them the nominal's schedule and
+    the problem's initial velocity."""
+
+    def __init__(self, problem, spec, precision: str = "fp64", store_ip_data: bool = True, device: int = 0,
+                 graph_steps: int = 50):
+        lib = library()
+        ne, na = spec.num_exact, spec.num_approx
+        S = 1 + ne + na
+        N, E = problem.num_nodes, problem.num_elem
+        self.spec, self.num_trajectories, self.mesh_problem = spec, S, problem
+        self.problems = [problem] * S
+        self.problem = Problem(coords=np.concatenate([problem.coords] * S),
+                               conn=np.concatenate([problem.conn + k * N for k in range(1 + ne)]).astype(np.int32),
+                               node_sets={}, density=problem.density, bulk_modulus=problem.bulk_modulus,
+                               shear_modulus=problem.shear_modulus, bcs=[],
+                               v_init=None if problem.v_init is None else np.concatenate([problem.v_init] * S))
+        self.precision = precision
+        mats = problem.materials()
+        bm = (_AnyMaterial * len(mats))()
+        for b, mt in enumerate(mats):
+            bm[b] = _AnyMaterial(mt.MODELS[mt.model], 0, mt.density, mt.bulk_modulus, mt.shear_modulus)
+        prm = spec.sample_parameters(problem)
+        kb = np.ascontiguousarray(prm["bulk_modulus"][:ne])
+        ks = np.ascontiguousarray(prm["shear_modulus"][:ne])
+        cf = np.ascontiguousarray(spec.coefficients, dtype=np.float64)
+        coords = np.ascontiguousarray(problem.coords, dtype=np.float64)
+        conn = np.ascontiguousarray(problem.conn, dtype=np.int32)
+        eb = np.ascontiguousarray(problem.elem_block, dtype=np.int32) if len(mats) > 1 else None
+        self._keep = [coords, conn, kb, ks, cf, eb]
+        mesh = _Mesh(N, E, _d(coords), conn.ctypes.data_as(_ip))
+        opt = _Options(PRECISION[precision], 1 if store_ip_data else 0, device, graph_steps)
+        h = _vp()
+        _check(lib.nsm_create_uq(C.byref(mesh), len(mats), None if eb is None else eb.ctypes.data_as(_ip), bm, ne,
+                                 _d(kb), _d(ks), na, _d(cf), C.byref(opt), C.byref(h)))
+        self._h = h
+        no, eo = np.zeros(S + 1, np.int32), np.zeros(S + 1, np.int32)
+        _check(lib.nsm_ensemble_offsets(h, no.ctypes.data_as(_ip), eo.ctypes.data_as(_ip)))
+        self.node_offsets, self.elem_offsets = no, eo
+        for t in range(S):
+            for bc in problem.bcs:
+                if bc.node_set not in problem.node_sets:
+                    continue
+                if bc.kind == BC_PRESCRIBED_DISPLACEMENT and t > 0:
+                    continue
+                nodes = np.ascontiguousarray(np.asarray(problem.node_sets[bc.node_set]) + no[t], dtype=np.int32)
+                _check(lib.nsm_add_boundary_condition(h, bc.kind, bc.component, bc.value,
+                                                      nodes.ctypes.data_as(_ip), len(nodes)))
+
+    def trajectories(self, label):
+        """A nodal vector field of every trajectory: [trajectories, N, 3]
+        (nominal, exact samples, approximate samples)."""
+        return self.GetVectorNodeData(label).reshape(self.num_trajectories, self.mesh_problem.num_nodes, 3)
 
 
 def _concatenate(problems):

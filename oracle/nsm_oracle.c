@@ -1018,6 +1018,175 @@ nsm_oracle_continue(
   return rc;
 }
 
+/* ---- The reference's UQ mode ----
+ * nimble_uq::ModelData (src/uq/nimble_uq_model_data.cc:55-248) with UqModel
+ * (src/uq/nimble_uq.cc:270-345) on one mesh: the nominal trajectory, num_exact
+ * off-nominal trajectories that evaluate the element forces with their own
+ * moduli (nimble_uq::Block::ComputeInternalForce with alternative
+ * parameters, src/uq/nimble_uq_block.cc:57-164), and num_approx trajectories
+ * whose force is the linear closure of the nominal and exact forces
+ * (UqModel::ApplyClosure, src/uq/nimble_uq.cc:327-345).  The explicit
+ * integrator drives them through the ModelData hooks it calls every step. */
+
+/* Velocity-type conditions act on every trajectory, displacement-type ones
+ * on the nominal only (src/nimble_boundary_condition_manager.h:137-206). */
+static void
+apply_kinematic_uq(const nsm_oracle_model* m, double t_cur, double t_prev, const double* u, double* v, int ns,
+                   double** sv)
+{
+  double delta_t = t_cur - t_prev;
+  for (int b = 0; b < m->num_bcs; b++) {
+    int c = m->bc_component[b];
+    if (m->bc_kind[b] == NSM_ORACLE_PRESCRIBED_VELOCITY) {
+      for (int k = m->bc_ptr[b]; k < m->bc_ptr[b + 1]; k++) {
+        v[3 * m->bc_nodes[k] + c] = m->bc_value[b];
+        for (int s = 0; s < ns; s++) sv[s][3 * m->bc_nodes[k] + c] = m->bc_value[b];
+      }
+    } else if (m->bc_kind[b] == NSM_ORACLE_PRESCRIBED_DISPLACEMENT && delta_t > 0.0) {
+      for (int k = m->bc_ptr[b]; k < m->bc_ptr[b + 1]; k++) {
+        int n        = m->bc_nodes[k];
+        v[3 * n + c] = (m->bc_value[b] - u[3 * n + c]) / delta_t;
+      }
+    }
+  }
+}
+
+/* ModelData::UpdateWithNewVelocity / UpdateWithNewDisplacement of the UQ
+ * trajectories (src/uq/nimble_uq_model_data.cc:218-246). */
+static void
+uq_velocity(const double* mass, long n3, int ns, double** sf, double** sv, double dt)
+{
+  for (int s = 0; s < ns; s++)
+    for (long i = 0; i < n3; i++) {
+      const double mi = mass[i / 3];
+      const double a  = (1.0 / mi) * (sf[s][i] + 0.0);
+      sv[s][i] += dt * a;
+    }
+}
+
+int
+nsm_oracle_run_uq(
+    const nsm_oracle_model* m,
+    int                     num_exact,
+    const double*           exact_bulk,
+    const double*           exact_shear,
+    int                     num_approx,
+    const double*           coef,
+    double                  final_time,
+    int                     num_steps,
+    int                     output_frequency,
+    const double*           v_init,
+    int                     num_threads,
+    int                     max_outputs,
+    double*                 out_u,
+    double*                 out_v,
+    double*                 out_f,
+    double*                 out_su,
+    double*                 out_sv,
+    double*                 out_sf,
+    int*                    out_num_outputs)
+{
+  build_tables();
+  const int  ns = num_exact + num_approx, B = m->num_blocks > 1 ? m->num_blocks : 1;
+  const long n3 = 3L * m->num_nodes;
+  nsm_oracle* o = nsm_oracle_create(m, num_threads);
+  if (!o) return -2;
+  nsm_oracle_begin(o, final_time, num_steps, output_frequency, NULL);
+  nsm_oracle_model* mk = (nsm_oracle_model*)calloc((size_t)(num_exact > 0 ? num_exact : 1), sizeof(nsm_oracle_model));
+  work*             wk = (work*)calloc((size_t)(num_exact > 0 ? num_exact : 1), sizeof(work));
+  double**          su = (double**)calloc((size_t)(ns > 0 ? ns : 1), sizeof(double*));
+  double**          sv = (double**)calloc((size_t)(ns > 0 ? ns : 1), sizeof(double*));
+  double**          sf = (double**)calloc((size_t)(ns > 0 ? ns : 1), sizeof(double*));
+  int               rc = 0;
+  for (int s = 0; s < ns; s++) {
+    su[s] = (double*)calloc((size_t)n3, sizeof(double));
+    sv[s] = (double*)calloc((size_t)n3, sizeof(double));
+    sf[s] = (double*)calloc((size_t)n3, sizeof(double));
+  }
+  for (int k = 0; k < num_exact; k++) {
+    mk[k] = *m;
+    if (m->num_blocks > 1) {
+      mk[k].block_bulk  = exact_bulk + (size_t)k * B;
+      mk[k].block_shear = exact_shear + (size_t)k * B;
+    } else {
+      mk[k].bulk_modulus  = exact_bulk[k];
+      mk[k].shear_modulus = exact_shear[k];
+    }
+    if (work_init(&wk[k], &mk[k])) rc = -2;
+  }
+  if (rc == 0) {
+    /* initial conditions of every trajectory */
+    for (int s = 0; s < ns; s++) apply_initial(m, sv[s]);
+    if (v_init)
+      for (int s = 0; s < ns; s++) memcpy(sv[s], v_init, (size_t)n3 * sizeof(double));
+    if (v_init) memcpy(o->v, v_init, (size_t)n3 * sizeof(double));
+    apply_kinematic_uq(m, 0.0, 0.0, o->u, o->v, ns, sv);
+  }
+  const double* mass     = o->w.mass;
+  int           recorded = 0;
+  for (int step_i = 0; rc == 0 && step_i < num_steps; step_i++) {
+    int is_output = 0;
+    if (output_frequency != 0 && (step_i % output_frequency == 0 || step_i == num_steps - 1)) is_output = 1;
+    o->t_prev = o->t_cur;
+    o->t_cur += o->dt_user;
+    const double delta = o->t_cur - o->t_prev, half = 0.5 * delta;
+    for (long i = 0; i < n3; i++) o->v[i] += half * o->a[i];
+    uq_velocity(mass, n3, ns, sf, sv, half);
+    apply_kinematic_uq(m, o->t_cur, o->t_prev, o->u, o->v, ns, sv);
+    for (long i = 0; i < n3; i++) o->u[i] += delta * o->v[i];
+    for (int s = 0; s < ns; s++)
+      for (long i = 0; i < n3; i++) su[s][i] += delta * sv[s][i];
+    apply_kinematic_uq(m, o->t_cur, o->t_prev, o->u, o->v, ns, sv);
+    internal_force(&o->w, o->u, o->f_int, o->num_threads);
+    for (int k = 0; k < num_exact; k++) internal_force(&wk[k], su[k], sf[k], o->num_threads);
+    for (int s = 0; s < num_approx; s++) {
+      double*       f = sf[num_exact + s];
+      const double* c = coef + (size_t)s * (num_exact + 1);
+      for (long i = 0; i < n3; i++) {
+        f[i] = o->f_int[i] * c[0];
+        for (int k = 0; k < num_exact; k++) f[i] += sf[k][i] * c[k + 1];
+      }
+    }
+    for (int i = 0; i < m->num_nodes; i++) {
+      const double oneOverM = 1.0 / mass[i];
+      for (int k = 0; k < 3; k++) o->a[3 * i + k] = oneOverM * (o->f_int[3 * i + k] + 0.0);
+    }
+    for (long i = 0; i < n3; i++) o->v[i] += half * o->a[i];
+    uq_velocity(mass, n3, ns, sf, sv, half);
+    if (is_output) apply_kinematic_uq(m, o->t_cur, o->t_prev, o->u, o->v, ns, sv);
+    if ((is_output || (output_frequency == 0 && step_i == num_steps - 1)) && recorded < max_outputs) {
+      const size_t t = (size_t)recorded;
+      if (out_u) memcpy(out_u + t * n3, o->u, (size_t)n3 * sizeof(double));
+      if (out_v) memcpy(out_v + t * n3, o->v, (size_t)n3 * sizeof(double));
+      if (out_f) memcpy(out_f + t * n3, o->f_int, (size_t)n3 * sizeof(double));
+      for (int s = 0; s < ns; s++) {
+        const size_t base = (t * ns + s) * (size_t)n3;
+        if (out_su) memcpy(out_su + base, su[s], (size_t)n3 * sizeof(double));
+        if (out_sv) memcpy(out_sv + base, sv[s], (size_t)n3 * sizeof(double));
+        if (out_sf) memcpy(out_sf + base, sf[s], (size_t)n3 * sizeof(double));
+      }
+      recorded++;
+    }
+  }
+  if (o->w.bad_jacobian) rc = -1;
+  for (int k = 0; k < num_exact; k++)
+    if (wk[k].bad_jacobian) rc = -1;
+  if (out_num_outputs) *out_num_outputs = recorded;
+  for (int k = 0; k < num_exact; k++) work_free(&wk[k]);
+  for (int s = 0; s < ns; s++) {
+    free(su[s]);
+    free(sv[s]);
+    free(sf[s]);
+  }
+  free(su);
+  free(sv);
+  free(sf);
+  free(wk);
+  free(mk);
+  nsm_oracle_destroy(o);
+  return rc;
+}
+
 /* Extended-precision Cauchy stress of the displacement field u at the
  * integration points of the listed elements (long double: at least a 64-bit
  * significand).  The same constitutive law as the reference

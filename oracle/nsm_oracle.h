@@ -104,6 +104,20 @@ void nsm_oracle_volume_average(const double* x, int nq, const double* q, double*
 void   nsm_oracle_lumped_mass(const nsm_oracle_model* m, double* mass);
 double nsm_oracle_critical_time_step(const nsm_oracle_model* m);
 
+/* The reference's UQ mode (src/uq/nimble_uq_model_data.cc:55-248,
+ * src/uq/nimble_uq.cc:270-345): the nominal trajectory of m, num_exact
+ * trajectories with moduli exact_bulk / exact_shear [num_exact][blocks], and
+ * num_approx trajectories driven by the closure coef [num_approx][num_exact+1]
+ * (nominal first).  v_init (nullable) is every trajectory's initial velocity.
+ * Records after every output step (the last step when output_frequency is 0),
+ * at most max_outputs: nominal u, v, f [T][N][3]; samples su, sv, sf
+ * [T][num_exact + num_approx][N][3], exact first.  0, or -1 on an inverted
+ * element. */
+int nsm_oracle_run_uq(const nsm_oracle_model* m, int num_exact, const double* exact_bulk, const double* exact_shear,
+                      int num_approx, const double* coef, double final_time, int num_steps, int output_frequency,
+                      const double* v_init, int num_threads, int max_outputs, double* out_u, double* out_v,
+                      double* out_f, double* out_su, double* out_sv, double* out_sf, int* out_num_outputs);
+
 /* Derived element output over a model (src/nimble_block.cc:438-497): u [N][3],
  * sigma [E][8][6], F [E][8][9] -> volume [E], avg_sigma [E][6], avg_F [E][9]. */
 void nsm_oracle_derived_element_data(const nsm_oracle_model* m, const double* u, const double* sigma, const double* F,

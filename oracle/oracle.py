@@ -99,9 +99,30 @@ def port():
         lib.nsm_oracle_energies.argtypes = [C.c_void_p, _dp, _dp]
         lib.nsm_oracle_stress_exact.argtypes = [C.POINTER(_Model), _dp, C.c_int, _ip, _dp]
         lib.nsm_oracle_volume_average.argtypes = [_dp, C.c_int, _dp, _dp, _dp]
+        lib.nsm_oracle_run_uq.argtypes = [C.POINTER(_Model), C.c_int, _dp, _dp, C.c_int, _dp, C.c_double, C.c_int,
+                                          C.c_int, _dp, C.c_int, C.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _ip]
         lib.nsm_oracle_derived_element_data.argtypes = [C.POINTER(_Model), _dp, _dp, _dp, _dp, _dp, _dp]
         _port = lib
     return _port
+
+
+REF_UQ_SO = os.path.join(HERE, "_ref", "libnimble_ref_uq.so")
+_ref_uq = None
+
+
+def ref_uq():
+    """The reference built with its UQ mode (oracle/_ref/libnimble_ref_uq.so)."""
+    global _ref_uq
+    if _ref_uq is None:
+        if not os.path.exists(REF_UQ_SO):
+            raise RuntimeError("UQ reference library not built (oracle/_ref); needs the reference sources")
+        lib = C.CDLL(REF_UQ_SO)
+        lib.nimref_run_uq.argtypes = [C.c_int, _dp, C.c_int, _ip, C.c_int, _ip, C.c_char_p, C.c_int, _ip, _ip,
+                                      C.c_char_p, C.c_char_p, C.c_double, C.c_int, C.c_int, _dp, C.c_char_p,
+                                      C.c_char_p, C.c_int, C.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _ip]
+        lib.nimref_last_error.restype = C.c_char_p
+        _ref_uq = lib
+    return _ref_uq
 
 
 def reference_available() -> bool:
@@ -271,6 +292,81 @@ def run_ref_outputs(problem, final_time, num_steps, output_frequency=0, with_ip=
         st.update(mass=mass, dt_crit=dt.value, loop_seconds=secs.value)
         states.append(st)
     return states
+
+
+def _uq_outputs(problem, spec, num_steps, output_frequency):
+    N = problem.num_nodes
+    of = int(output_frequency)
+    T = 1 if of == 0 else (int(num_steps) + of - 1) // of + 1
+    S = spec.num_exact + spec.num_approx
+    return T, {"u": np.zeros((T, N, 3)), "v": np.zeros((T, N, 3)), "f": np.zeros((T, N, 3)),
+               "su": np.zeros((T, S, N, 3)), "sv": np.zeros((T, S, N, 3)), "sf": np.zeros((T, S, N, 3))}
+
+
+def run_port_uq(problem, spec, final_time, num_steps, output_frequency=0, threads=1):
+    """The C restatement of the reference's UQ mode (nsm_oracle_run_uq): the
+    nominal trajectory (u, v, f [T,N,3]) and the samples (su, sv, sf
+    [T,S,N,3], exact first) after every output step."""
+    keep = []
+    m = _model(problem, keep)
+    prm = spec.sample_parameters(problem)
+    ne = spec.num_exact
+    kb = np.ascontiguousarray(prm["bulk_modulus"][:ne])
+    ks = np.ascontiguousarray(prm["shear_modulus"][:ne])
+    cf = np.ascontiguousarray(spec.coefficients)
+    T, out = _uq_outputs(problem, spec, num_steps, output_frequency)
+    v0 = None if problem.v_init is None else np.ascontiguousarray(problem.v_init, dtype=np.float64)
+    n = C.c_int(0)
+    rc = port().nsm_oracle_run_uq(C.byref(m), ne, _d(kb), _d(ks), spec.num_approx, _d(cf), float(final_time),
+                                  int(num_steps), int(output_frequency), _d(v0), int(threads), T, _d(out["u"]),
+                                  _d(out["v"]), _d(out["f"]), _d(out["su"]), _d(out["sv"]), _d(out["sf"]),
+                                  C.byref(n))
+    if rc != 0:
+        raise RuntimeError(f"oracle UQ run failed ({rc})")
+    return {k: v[: n.value] for k, v in out.items()}
+
+
+def run_ref_uq(problem, spec, final_time, num_steps, output_frequency=0, workdir="."):
+    """The reference's own UQ mode (nimble_uq::ModelData through the
+    harness): same outputs as run_port_uq.  The samples file is written into
+    workdir, which is also the working directory during the run (the
+    reference writes parameter_samples.dat there)."""
+    lib = ref_uq()
+    names = list(problem.node_sets.keys())
+    ns_ptr = np.zeros(len(names) + 1, np.int32)
+    parts = []
+    for s, nm in enumerate(names):
+        ids = np.asarray(problem.node_sets[nm], np.int32)
+        parts.append(ids)
+        ns_ptr[s + 1] = ns_ptr[s] + len(ids)
+    ns_nodes = np.concatenate(parts).astype(np.int32) if parts else np.zeros(0, np.int32)
+    bcs = "\n".join(bc.line() for bc in problem.bcs)
+    coords = np.ascontiguousarray(problem.coords, dtype=np.float64)
+    conn = np.ascontiguousarray(problem.conn, dtype=np.int32)
+    mats = problem.materials()
+    eb = np.ascontiguousarray(problem.elem_block, dtype=np.int32) if len(mats) > 1 else None
+    v0 = None if problem.v_init is None else np.ascontiguousarray(problem.v_init, dtype=np.float64)
+    T, out = _uq_outputs(problem, spec, num_steps, output_frequency)
+    workdir = os.path.abspath(workdir)
+    samples = os.path.join(workdir, "uq_samples.txt")
+    with open(samples, "w") as f:
+        f.write(spec.samples_text())
+    mass, dt, n = np.zeros(problem.num_nodes), C.c_double(0.0), C.c_int(0)
+    cwd = os.getcwd()
+    os.chdir(workdir)
+    try:
+        rc = lib.nimref_run_uq(problem.num_nodes, _d(coords), problem.num_elem, _i(conn), len(mats), _i(eb),
+                               "\n".join(mt.line() for mt in mats).encode(), len(names), _i(ns_ptr), _i(ns_nodes),
+                               "\n".join(names).encode(), bcs.encode(), float(final_time), int(num_steps),
+                               int(output_frequency), _d(v0), "\n".join(spec.parameter_lines()).encode(),
+                               samples.encode(), spec.num_exact + spec.num_approx, T, _d(out["u"]), _d(out["v"]),
+                               _d(out["f"]), _d(out["su"]), _d(out["sv"]), _d(out["sf"]), _d(mass),
+                               C.cast(C.pointer(dt), _dp), C.byref(n))
+    finally:
+        os.chdir(cwd)
+    if rc != 0:
+        raise RuntimeError("reference UQ run failed: " + lib.nimref_last_error().decode())
+    return {k: v[: n.value] for k, v in out.items()}
 
 
 def run_ref(problem, final_time, num_steps, output_frequency=0, with_ip=True):

@@ -178,8 +178,8 @@ nimref_last_error()
  * Also the lumped mass [N], the critical time step, the wall seconds of the
  * step loop and the number of recorded outputs.  Returns 0, or -1 with
  * nimref_last_error() set. */
-int
-nimref_run_blocks(
+static int
+run_impl(
     int           num_nodes,
     const double* xyz,
     int           num_elem,
@@ -206,7 +206,13 @@ nimref_run_blocks(
     double*       out_mass,
     double*       out_dt_crit,
     double*       out_loop_seconds,
-    int*          out_num_outputs)
+    int*          out_num_outputs,
+    const char*   uq_params,     // "uq parameters" lines, or null (no UQ)
+    const char*   uq_samples,    // the UQ samples file
+    int           num_samples,   // exact + approximate samples expected
+    double*       out_su,        // [output][sample][N][3], exact samples first
+    double*       out_sv,
+    double*       out_sf)
 {
   try {
     HarnessMesh mesh;
@@ -232,6 +238,15 @@ nimref_run_blocks(
     }
     parser.Set("output fields", "displacement");
     for (auto const& bc : SplitLines(bcs)) parser.Set("boundary condition", bc);
+    if (uq_params) {
+#ifdef NIMBLE_HAVE_UQ
+      parser.SetToUseUQ();  // what the command line's UQ flag sets (src/nimble_parser.h:276-279)
+      for (auto const& line : SplitLines(uq_params)) parser.Set("uq parameters", line);
+      parser.Set("uq model", std::string("file ") + uq_samples);
+#else
+      throw std::invalid_argument("this build has no UQ mode");
+#endif
+    }
 
     nimble::DataManager data_manager(parser, mesh);
     auto                model_data_ptr = data_manager.GetModelData();
@@ -258,10 +273,33 @@ nimref_run_blocks(
     int    num_load_steps           = parser.NumLoadSteps();
     double user_specified_time_step = (parser.FinalTime() - initial_time) / num_load_steps;
 
+    // UQ trajectories (nimble_uq::ModelData, src/uq/nimble_uq.cc:282-326):
+    // exact samples, then approximate samples
+    std::vector<double*> su, sv, sf;
+    if (uq_params) {
+      const char* kinds[2] = {"exact", "sample"};
+      for (const char* kind : kinds) {
+        for (int i = 1;; i++) {
+          const std::string tag = "_" + std::to_string(i);
+          const int         id  = host_model.GetFieldId(std::string(kind) + "_displacement" + tag);
+          if (id < 0) break;
+          su.push_back(host_model.GetNodeData(id));
+          sv.push_back(host_model.GetNodeData(host_model.GetFieldId(std::string(kind) + "_velocity" + tag)));
+          sf.push_back(host_model.GetNodeData(host_model.GetFieldId(std::string(kind) + "_force" + tag)));
+        }
+      }
+      if (static_cast<int>(su.size()) != num_samples) throw std::invalid_argument("unexpected number of UQ samples");
+    }
+
     model_data.ApplyInitialConditions(data_manager);
     if (v_init != nullptr) {
+      // the initial velocity of every trajectory, as an initial_velocity
+      // condition would set it (src/nimble_boundary_condition_manager.h:93-123)
       for (int i = 0; i < num_nodes; i++)
-        for (int k = 0; k < 3; k++) velocity(i, k) = v_init[3 * i + k];
+        for (int k = 0; k < 3; k++) {
+          velocity(i, k) = v_init[3 * i + k];
+          for (double* s_v : sv) s_v[3 * i + k] = v_init[3 * i + k];
+        }
     }
     model_data.ApplyKinematicConditions(data_manager, 0.0, 0.0);
 
@@ -281,6 +319,12 @@ nimref_run_blocks(
           if (out_a) out_a[j] = acceleration(i, k);
           if (out_fint) out_fint[j] = internal_force(i, k);
         }
+      }
+      for (size_t smp = 0; smp < su.size(); smp++) {
+        const size_t base = (o * su.size() + smp) * 3 * static_cast<size_t>(num_nodes);
+        if (out_su) std::memcpy(out_su + base, su[smp], 3 * sizeof(double) * num_nodes);
+        if (out_sv) std::memcpy(out_sv + base, sv[smp], 3 * sizeof(double) * num_nodes);
+        if (out_sf) std::memcpy(out_sf + base, sf[smp], 3 * sizeof(double) * num_nodes);
       }
       if (out_F || out_sigma) {
         for (int b = 0; b < num_blocks; b++) {
@@ -350,6 +394,91 @@ nimref_run_blocks(
     return -1;
   }
 }
+
+int
+nimref_run_blocks(
+    int           num_nodes,
+    const double* xyz,
+    int           num_elem,
+    const int*    conn,
+    int           num_blocks,
+    const int*    elem_block,
+    const char*   materials,
+    int           num_node_sets,
+    const int*    ns_ptr,
+    const int*    ns_nodes,
+    const char*   ns_names,
+    const char*   bcs,
+    double        final_time,
+    int           num_steps,
+    int           output_frequency,
+    const double* v_init,
+    int           max_outputs,
+    double*       out_u,
+    double*       out_v,
+    double*       out_a,
+    double*       out_fint,
+    double*       out_F,
+    double*       out_sigma,
+    double*       out_mass,
+    double*       out_dt_crit,
+    double*       out_loop_seconds,
+    int*          out_num_outputs)
+{
+  return run_impl(num_nodes, xyz, num_elem, conn, num_blocks, elem_block, materials, num_node_sets, ns_ptr, ns_nodes,
+                  ns_names, bcs, final_time, num_steps, output_frequency, v_init, max_outputs, out_u, out_v, out_a,
+                  out_fint, out_F, out_sigma, out_mass, out_dt_crit, out_loop_seconds, out_num_outputs, nullptr,
+                  nullptr, 0, nullptr, nullptr, nullptr);
+}
+
+#ifdef NIMBLE_HAVE_UQ
+/* The reference's UQ mode (nimble_uq::ModelData, src/uq/nimble_uq_model_data.cc:145-248,
+ * and UqModel, src/uq/nimble_uq.cc): as nimref_run_blocks, with the
+ * "uq parameters" lines (one per material, "material_<b> <param> <range> ...")
+ * and the samples file (src/uq/nimble_uq.cc:145-218).  The nominal
+ * trajectory is out_u / out_v / out_fint; out_su, out_sv, out_sf
+ * [output][sample][N][3] hold the exact samples and then the approximate
+ * samples (num_samples in all).  v_init, when given, is every trajectory's
+ * initial velocity.  The reference writes parameter_samples.dat into the
+ * working directory. */
+int
+nimref_run_uq(
+    int           num_nodes,
+    const double* xyz,
+    int           num_elem,
+    const int*    conn,
+    int           num_blocks,
+    const int*    elem_block,
+    const char*   materials,
+    int           num_node_sets,
+    const int*    ns_ptr,
+    const int*    ns_nodes,
+    const char*   ns_names,
+    const char*   bcs,
+    double        final_time,
+    int           num_steps,
+    int           output_frequency,
+    const double* v_init,
+    const char*   uq_params,
+    const char*   uq_samples,
+    int           num_samples,
+    int           max_outputs,
+    double*       out_u,
+    double*       out_v,
+    double*       out_fint,
+    double*       out_su,
+    double*       out_sv,
+    double*       out_sf,
+    double*       out_mass,
+    double*       out_dt_crit,
+    int*          out_num_outputs)
+{
+  return run_impl(num_nodes, xyz, num_elem, conn, num_blocks, elem_block, materials, num_node_sets, ns_ptr, ns_nodes,
+                  ns_names, bcs, final_time, num_steps, output_frequency, v_init, max_outputs, out_u, out_v, nullptr,
+                  out_fint, nullptr, nullptr, out_mass, out_dt_crit, nullptr, out_num_outputs, uq_params, uq_samples,
+                  num_samples, out_su, out_sv, out_sf);
+}
+#endif
 
 /* One block of one material; the state after the last step only (see
  * nimref_run_blocks).  material: "<model> density .. bulk_modulus .. shear_modulus ..". */

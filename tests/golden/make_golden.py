@@ -198,6 +198,42 @@ def ref_derived_fixture(name="cube4_jitter"):
     print("wrote derived", name)
 
 
+def ref_uq_fixture(name="uq_wave", keep_every=10):
+    """The reference's UQ regression deck (test/uq/uq_wave: nominal, 2 exact and
+    5 approximate trajectories, 10,000 steps; its gold file is not in the
+    repository) run by the reference's own UQ mode (nimble_uq::ModelData
+    through the harness): every keep_every-th output step of every
+    trajectory, with the deck's mesh, materials, conditions and UQ input."""
+    import tempfile
+    from nimblesm_gb300.uq import UqSpec
+    base = os.path.join(REF, "test", "uq", name)
+    deck = parse_deck(os.path.join(base, f"{name}.in"))
+    mesh = read_genesis(os.path.join(base, deck.genesis_file))
+    p = deck.problem(mesh)
+    uq_lines = [ln.split(":", 1)[1].strip() for ln in open(os.path.join(base, f"{name}.in"))
+                if ln.split(":", 1)[0].strip() == "uq parameters"]
+    samples = open(os.path.join(base, deck.keys["uq model"].split()[1])).read()
+    mat_block = {deck.blocks[f"block_{int(b)}"]: i for i, b in enumerate(mesh["block_ids"])}
+    spec = UqSpec.parse(uq_lines, samples, mat_block)
+    with tempfile.TemporaryDirectory() as wd:
+        r = O.run_ref_uq(p, spec, deck.final_time, deck.num_steps, deck.output_frequency, workdir=wd)
+    out_steps = [s + 1 for s in range(deck.num_steps)
+                 if deck.output_frequency != 0 and (s % deck.output_frequency == 0 or s == deck.num_steps - 1)]
+    keep = list(range(0, len(out_steps), keep_every))
+    if keep[-1] != len(out_steps) - 1:
+        keep.append(len(out_steps) - 1)
+    fx = {"coords": mesh["coords"], "conn": mesh["conn"], "ns_names": np.array(list(mesh["node_sets"])),
+          "bc_lines": np.array(deck.bcs), "material_line": p.material_line(), "final_time": deck.final_time,
+          "num_steps": deck.num_steps, "output_frequency": deck.output_frequency,
+          "uq_parameters": np.array(uq_lines), "uq_samples": samples, "out_steps": np.array(out_steps)[keep]}
+    for nm, ids in mesh["node_sets"].items():
+        fx["ns:" + nm] = ids
+    for k, v in r.items():
+        fx[k] = v[keep]
+    np.savez_compressed(os.path.join(HERE, f"ref_{name}.npz"), **fx)
+    print("wrote UQ", name, fx["out_steps"])
+
+
 def ref_points_fixture():
     """Stress and single-element known answers from the reference."""
     rng = np.random.default_rng(2024)
@@ -287,3 +323,4 @@ if __name__ == "__main__":
     ref_gold_rerun()
     ref_envelope_fixture("cube40_schedule", 40, 0.2, 0, 2000)
     ref_derived_fixture("cube4_jitter")
+    ref_uq_fixture("uq_wave")

@@ -54,6 +54,19 @@ def gold_checks(fx, t, st, vol, sig_avg, F_avg):
         assert exodiff_ok(sig_avg, fx["gold:sigma_avg"][t + 1], fx["tol:sigma_avg"])
 
 
+def uq_problem(fx):
+    """Problem and UqSpec of the UQ fixture (one block, material_1)."""
+    from nimblesm_gb300.uq import UqSpec
+    w = str(fx["material_line"]).split()
+    prm = {w[i]: float(w[i + 1]) for i in range(1, len(w) - 1, 2)}
+    names = [str(s) for s in fx["ns_names"]]
+    p = Problem(coords=fx["coords"], conn=fx["conn"], node_sets={n: fx["ns:" + n] for n in names},
+                density=prm["density"], bulk_modulus=prm["bulk_modulus"], shear_modulus=prm["shear_modulus"],
+                material_model=w[0], bcs=[BoundaryCondition.parse(str(b)) for b in fx["bc_lines"]])
+    spec = UqSpec.parse([str(x) for x in fx["uq_parameters"]], str(fx["uq_samples"]), {"material_1": 0})
+    return p, spec
+
+
 def output_steps(num_steps, output_frequency):
     """1-based step counts after which the reference writes output
     (src/integrators/explicit_time_integrator.cc:192-194)."""

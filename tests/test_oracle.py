@@ -5,7 +5,7 @@ import pytest
 
 from nimblesm_gb300.mesh import cube_problem, critical_time_step
 from oracle import oracle as O
-from tests.goldens import GOLD_DECKS, exodiff_ok, gold_checks, gold_problem, load, output_steps
+from tests.goldens import GOLD_DECKS, exodiff_ok, gold_checks, gold_problem, load, output_steps, uq_problem
 
 
 @pytest.fixture(scope="module", autouse=True)
@@ -58,6 +58,21 @@ def test_derived_element_data_matches_reference_bitwise():
     assert np.array_equal(avg, dx["stress"])
     assert np.array_equal(avg_F, dx["deformation_gradient"])
     assert abs(vol.sum() - 1.0) < 1e-3  # the unit cube, slightly deformed
+
+
+def test_uq_closure_matches_reference_bitwise():
+    """The reference's UQ regression deck (uq_wave: nominal, 2 exact and 5
+    approximate trajectories with the linear force closure, 10,000 steps):
+    the oracle's restatement against the reference's own UQ mode, every
+    trajectory, bit for bit."""
+    fx = load("ref_uq_wave")
+    p, spec = uq_problem(fx)
+    steps, of = int(fx["num_steps"]), int(fx["output_frequency"])
+    r = O.run_port_uq(p, spec, float(fx["final_time"]), steps, of)
+    idx = [output_steps(steps, of).index(int(s)) for s in fx["out_steps"]]
+    assert spec.num_exact == 2 and spec.num_approx == 5
+    for k in ("u", "v", "f", "su", "sv", "sf"):
+        assert np.array_equal(r[k][idx], fx[k]), k
 
 
 def test_numpy_critical_time_step_matches_oracle():

@@ -40,9 +40,9 @@ METRIC = "hex8 IP stress updates/sec, plain FP64 vs mixed/MLP at <=1e-3 rel. dis
 UNIT = "IP-updates/s"
 SCHEDULE_STEPS = 2000  # the workload's schedule: dt = 0.5 dt_crit, 2000 steps
 # FP64 flops per integration point of the FP64 element kernel's formulation:
-# 122.0 DFMA (2 flops each) + 31.5 DADD + 65.1 DMUL executed per point
+# 122.4 DFMA (2 flops each) + 22.8 DADD + 53.8 DMUL executed per point
 # (ncu on the 64^3 case, profiles/k_element_fp64_cube64.md).
-FP64_FLOPS_PER_IP = 340.6
+FP64_FLOPS_PER_IP = 321.2
 
 
 def algorithmic_bytes(N, E, precision):
@@ -446,16 +446,16 @@ def run_ours(args):
                           "rel_disp_err_vs_fp64": err, "after_steps": args.warmup + args.steps,
                           "element_launch_ms": r["prof"]["element_ms"] / max(r["prof"]["element_launches"], 1),
                           "clocks": r["clocks"]}
-    if args.uq_steps > 0:
+    if args.variants and args.uq_steps > 0:
         variants.update(uq_variants(E, args, local if ws > 1 else 0))
-    if args.big_steps > 0:
+    if args.variants and args.big_steps > 0:
         variants.update(big_fp32_variant(E, args, local if ws > 1 else 0))
     mlp = None
-    if args.mlp_steps > 0:
+    if args.variants and args.mlp_steps > 0:
         fp32_value = variants.get("fp32", {}).get("value", float("nan"))
         res, mlp = mlp_variant(E, args, problem, local if ws > 1 else 0, value / ws, fp32_value / ws)
         variants.update(res)
-    if args.acc_steps > 0:
+    if args.variants and args.acc_steps > 0:
         variants.update(accuracy_variant(E, args, problem, local if ws > 1 else 0, mlp))
     if mlp is not None:
         mlp.close()
@@ -480,7 +480,8 @@ def main():
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--n", type=int, default=128, help="cube divisions (default 128: 2,097,152 elements)")
     ap.add_argument("--precision", choices=("fp64", "fp32"), default="fp64")
-    ap.add_argument("--no-variants", dest="variants", action="store_false")
+    ap.add_argument("--no-variants", dest="variants", action="store_false",
+                    help="only the headline form (no FP32, ensemble, 256^3, closure or accuracy runs)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--uq-steps", type=int, default=100, help="timed steps of the 512-sample ensemble (0: skip)")
     ap.add_argument("--uq-samples", type=int, default=512)

@@ -20,6 +20,12 @@ __device__ __forceinline__ void store_vec(double* dst, const double* v, int n)
   for (int k = 0; k < n; k += 2) *reinterpret_cast<double2*>(dst + k) = make_double2(v[k], v[k + 1]);
 }
 
+// J > 0 without the FP64 pipe: the sign and magnitude bits of an IEEE number
+// order like a signed integer (a NaN J passes here and is caught as a
+// non-finite force).
+__device__ __forceinline__ bool positive(double x) { return __double_as_longlong(x) > 0; }
+__device__ __forceinline__ bool positive(float x) { return x > 0.0f; }
+
 // Nodal values of the element: FP64 form from the FP64 field, FP32 form from
 // the FP32 copy (no FP64 conversions, which would run on the FP64 pipe).
 template <typename T>
@@ -103,18 +109,23 @@ __device__ __forceinline__ void element_work(const ElementArgs& a, const int e)
 #pragma unroll
   for (int p = 0; p < 8; p++) {
     const int bit[3] = {sx_of(p), sy_of(p), sz_of(p)};
-    T         G0[3][3], det0;
+    T         G0[3][3], W0[3][3];  // J_X^{-1} and det J_X * J_X^{-1}
     if (kPrecomputedGeo) {
 #pragma unroll
-      for (int q = 0; q < 9; q++) G0[q / 3][q % 3] = T(__ldg(&a.geo[(p * 10 + q) * ld_e + e]));
-      det0 = T(__ldg(&a.geo[(p * 10 + 9) * ld_e + e]));
+      for (int q = 0; q < 9; q++) {
+        G0[q / 3][q % 3] = T(__ldg(&a.geo[(p * kGeoPerPoint + q) * ld_e + e]));
+        W0[q / 3][q % 3] = T(__ldg(&a.geo[(p * kGeoPerPoint + 10 + q) * ld_e + e]));
+      }
     } else {
-      T JX[3][3];
+      T JX[3][3], det0;
 #pragma unroll
       for (int i = 0; i < 3; i++)
 #pragma unroll
         for (int d = 0; d < 3; d++) JX[i][d] = GX[d][i][bit[other1(d)]][bit[other2(d)]];
       invert3<T>(JX, G0, det0);
+      if (!(det0 > T(0))) bad = true;  // (checked once at setup in the FP64 form)
+#pragma unroll
+      for (int q = 0; q < 9; q++) W0[q / 3][q % 3] = det0 * G0[q / 3][q % 3];
     }
     // H[i][J] = sum_d du_i/dxi_d G0[d][J]
     T H[3][3];
@@ -129,7 +140,7 @@ __device__ __forceinline__ void element_work(const ElementArgs& a, const int e)
       }
     T sig[6], C[3][3], J;
     material_stress<T>(model, H, K, Gm, sig, C, J);
-    if (!(J > T(0)) || !(det0 > T(0))) bad = true;  // inverted element
+    if (!positive(J)) bad = true;  // inverted element
     if (store) {
       T r[kIpRecord];
 #pragma unroll
@@ -141,7 +152,8 @@ __device__ __forceinline__ void element_work(const ElementArgs& a, const int e)
       r[15] = T(0);
       store_vec(rec + (size_t)p * ld_e * kIpRecord, r, kIpRecord);
     }
-    // P = sigma cof(F);  Q[d][i] = det J_X sum_J G0[d][J] P[i][J]
+    // P = sigma cof(F);  Q[d][i] = sum_J (det J_X J_X^{-1})[d][J] P[i][J],
+    // summed over the two points of each sign pair (the first assigns)
     T P[3][3];
 #pragma unroll
     for (int i = 0; i < 3; i++)
@@ -152,17 +164,14 @@ __device__ __forceinline__ void element_work(const ElementArgs& a, const int e)
     for (int d = 0; d < 3; d++)
 #pragma unroll
       for (int i = 0; i < 3; i++) {
-        T q = G0[d][0] * P[i][0] + G0[d][1] * P[i][1] + G0[d][2] * P[i][2];
-        S[d][i][bit[other1(d)]][bit[other2(d)]] += det0 * q;
+        T&      acc = S[d][i][bit[other1(d)]][bit[other2(d)]];
+        const T tail = first_of_pair(d, p) ? W0[d][2] * P[i][2] : fma(W0[d][2], P[i][2], acc);
+        acc          = fma(W0[d][0], P[i][0], fma(W0[d][1], P[i][1], tail));
       }
   }
 
-  // f_a,i = - sum_p sum_d dN_a/dxi_d(p) Q_p[d][i]
+  // f_a,i = - sum_p sum_d dN_a/dxi_d(p) Q_p[d][i]  (direction 0 assigns)
   T f[8][3];
-#pragma unroll
-  for (int n = 0; n < 8; n++)
-#pragma unroll
-    for (int i = 0; i < 3; i++) f[n][i] = T(0);
 #pragma unroll
   for (int d = 0; d < 3; d++) {
     const int o1 = other1(d), o2 = other2(d);
@@ -174,8 +183,10 @@ __device__ __forceinline__ void element_work(const ElementArgs& a, const int e)
       for (int b = 0; b < 2; b++)
 #pragma unroll
         for (int c = 0; c < 2; c++) {
-          f[corner_axes(d, 1, o1, b, o2, c)][i] -= R[b][c];
-          f[corner_axes(d, 0, o1, b, o2, c)][i] += R[b][c];
+          T& hi = f[corner_axes(d, 1, o1, b, o2, c)][i];
+          T& lo = f[corner_axes(d, 0, o1, b, o2, c)][i];
+          hi    = d == 0 ? -R[b][c] : hi - R[b][c];
+          lo    = d == 0 ? R[b][c] : lo + R[b][c];
         }
     }
   }
@@ -291,7 +302,7 @@ __global__ void __launch_bounds__(128) k_energy_partials(int N, long ld_n, const
     for (int p = 0; p < 8; p++) {
       const int bit[3] = {sx_of(p), sy_of(p), sz_of(p)};
       double    G0[3][3];
-      for (int q = 0; q < 9; q++) G0[q / 3][q % 3] = geo[(p * 10 + q) * ld_e + e];
+      for (int q = 0; q < 9; q++) G0[q / 3][q % 3] = geo[(p * kGeoPerPoint + q) * ld_e + e];
       double H[3][3];
       for (int i = 0; i < 3; i++)
         for (int J = 0; J < 3; J++) {
@@ -302,7 +313,8 @@ __global__ void __launch_bounds__(128) k_energy_partials(int N, long ld_n, const
           }
           H[i][J] = h;
         }
-      ie += geo[(p * 10 + 9) * ld_e + e] * (elastic_model ? energy_density_elastic(H, K, Gm) : energy_density(H, K, Gm));
+      ie += geo[(p * kGeoPerPoint + 9) * ld_e + e] *
+            (elastic_model ? energy_density_elastic(H, K, Gm) : energy_density(H, K, Gm));
     }
   }
   s_ke[threadIdx.x] = ke;

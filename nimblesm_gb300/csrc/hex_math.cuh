@@ -73,6 +73,15 @@ __device__ __forceinline__ void bwd_transform(const T S[2][2], T R[2][2])
   }
 }
 
+// Of the two points that share sign bits along the axes other than d (they
+// differ in the bit along d), whether p is the lower-numbered one: the first
+// to contribute to their sums.
+__host__ __device__ constexpr bool first_of_pair(int d, int p)
+{
+  return p < corner_of(d == 0 ? 1 - sx_of(p) : sx_of(p), d == 1 ? 1 - sy_of(p) : sy_of(p),
+                       d == 2 ? 1 - sz_of(p) : sz_of(p));
+}
+
 // Gradient values of a nodal field x[8][3]: G[d][i][s][t] = dx_i/dxi_d at the
 // points whose sign bits along the other axes of d are (s, t).
 template <typename T>
@@ -126,14 +135,13 @@ __device__ __forceinline__ void neohookean(const T H[3][3], T K, T G, T sig[6], 
   C[2][1] = F[0][2] * F[1][0] - F[0][0] * F[1][2];
   C[2][2] = F[0][0] * F[1][1] - F[0][1] * F[1][0];
   J       = F[0][0] * C[0][0] + F[0][1] * C[0][1] + F[0][2] * C[0][2];
-  // b - I = H + H^T + H H^T
+  // b - I = H + H^T + H H^T, one add and three fused multiply-adds per entry
   T B[6];
 #pragma unroll
   for (int q = 0; q < 6; q++) {
     const int i = q < 3 ? q : (q == 3 ? 0 : (q == 4 ? 1 : 2));
     const int j = q < 3 ? q : (q == 3 ? 1 : (q == 4 ? 2 : 0));
-    T t         = H[i][0] * H[j][0] + H[i][1] * H[j][1] + H[i][2] * H[j][2];
-    B[q]        = (H[i][j] + H[j][i]) + t;
+    B[q]        = fma(H[i][0], H[j][0], fma(H[i][1], H[j][1], fma(H[i][2], H[j][2], H[i][j] + H[j][i])));
   }
   const T r   = rcbrt_refined(J);
   const T r2  = r * r;
@@ -142,9 +150,10 @@ __device__ __forceinline__ void neohookean(const T H[3][3], T K, T G, T sig[6], 
   const T p   = T(0.5) * K * (J - r3);
   const T m   = (B[0] + B[1] + B[2]) * T(1.0 / 3.0);
   const T Gr5 = G * r5;
-  sig[0]      = p + Gr5 * (B[0] - m);
-  sig[1]      = p + Gr5 * (B[1] - m);
-  sig[2]      = p + Gr5 * (B[2] - m);
+  const T q0  = fma(-Gr5, m, p);  // p - G J^{-5/3} tr(b)/3
+  sig[0]      = fma(Gr5, B[0], q0);
+  sig[1]      = fma(Gr5, B[1], q0);
+  sig[2]      = fma(Gr5, B[2], q0);
   sig[3]      = Gr5 * B[3];
   sig[4]      = Gr5 * B[4];
   sig[5]      = Gr5 * B[5];

@@ -20,6 +20,11 @@ struct GroupMaterial {
   int    pad;
 };
 
+// Reference geometry per integration point (FP64 form), planes
+// [8 * kGeoPerPoint][ld_e]: per point J_X^{-1} (9, row-major), det J_X, and
+// det J_X * J_X^{-1} (9), the factor of the point's force term.
+constexpr int kGeoPerPoint = 19;
+
 struct SetupArgs {
   int           N, E;
   int           num_groups;      // samples; elements of sample g are [elem_off[g], elem_off[g+1])
@@ -31,7 +36,7 @@ struct SetupArgs {
   const double* X;         // [3][ld_n]
   const int*    node_ptr;  // [N+1]
   const int*    node_inc;  // 8*e + corner, increasing e per node
-  double*       geo;       // [80][ld_e]
+  double*       geo;       // [8 * kGeoPerPoint][ld_e]
   double*       me;        // [8][ld_e]
   double*       dt_elem;   // [E]
   double*       dt_partial;// [1024]
@@ -66,7 +71,7 @@ struct ElementArgs {
   const double* u;         // [3][ld_n] displacement (FP64 form)
   const float*  uf;        // [3][ld_n] FP32 copy of u (FP32 form)
   const float*  Xf;        // [3][ld_n] FP32 copy of X (FP32 form)
-  const double* geo;       // [80][ld_e] G0 and det J0 per ip (FP64 form only)
+  const double* geo;       // [8 * kGeoPerPoint][ld_e] (FP64 form only)
   double        bulk, shear;     // material when elem_group is null
   int           model;           // material model when elem_group is null
   const int*    elem_group;      // [E] material of each element, or null

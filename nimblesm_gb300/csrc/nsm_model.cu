@@ -68,7 +68,7 @@ struct nsm_model {
   double* d_fext = nullptr;
   double* d_mass = nullptr;
   double* d_inv_mass = nullptr;
-  double* d_geo = nullptr;  // [80][ld_e]
+  double* d_geo = nullptr;  // [8 * kGeoPerPoint][ld_e]
   void*   d_ip = nullptr;   // [8][ld_e][16] per-point F and sigma records
   void*   d_fe = nullptr;   // [ld_e][24] element nodal forces
   float*  d_Xf = nullptr;   // FP32 copies of X and u (FP32 form)
@@ -455,7 +455,7 @@ int create_impl(int S, const nsm_mesh_desc* meshes, int num_mats, const nsm_mate
   }
   NSM_CUDA_B(cudaMalloc(&m->d_mass, sizeof(double) * m->ld_n));
   NSM_CUDA_B(cudaMalloc(&m->d_inv_mass, sizeof(double) * m->ld_n));
-  NSM_CUDA_B(cudaMalloc(&m->d_geo, sizeof(double) * 80 * m->ld_e));
+  NSM_CUDA_B(cudaMalloc(&m->d_geo, sizeof(double) * 8 * nsm::kGeoPerPoint * m->ld_e));
   NSM_CUDA_B(cudaMalloc(&m->d_ip, eb * nsm::kIpRecord * 8 * m->ld_e));
   NSM_CUDA_B(cudaMalloc(&m->d_fe, eb * 24 * m->ld_e));
   NSM_CUDA_B(cudaMemsetAsync(m->d_ip, 0, eb * nsm::kIpRecord * 8 * m->ld_e, m->stream));

@@ -39,10 +39,12 @@ FALLBACK_HBM_GBS = 6800.0
 METRIC = "hex8 IP stress updates/sec, plain FP64 vs mixed/MLP at <=1e-3 rel. disp error"
 UNIT = "IP-updates/s"
 SCHEDULE_STEPS = 2000  # the workload's schedule: dt = 0.5 dt_crit, 2000 steps
-# FP64 flops per integration point of the FP64 element kernel's formulation:
-# 122.4 DFMA (2 flops each) + 22.8 DADD + 53.8 DMUL executed per point
-# (ncu on the 64^3 case, profiles/k_element_fp64_cube64.md).
-FP64_FLOPS_PER_IP = 321.2
+# FP64 work per integration point of the FP64 element kernel's formulation:
+# 95.4 DFMA (2 flops each) + 31.8 DADD + 54.7 DMUL executed per point (ncu on
+# the 64^3 case, profiles/k_element_fp64_cube64.md).  The FP64 pipe issues
+# 2 of these instructions per SM per cycle, whatever their kind.
+FP64_FLOPS_PER_IP = 277.2
+FP64_INSTR_PER_IP = 181.9
 
 
 def algorithmic_bytes(N, E, precision):
@@ -431,10 +433,13 @@ def run_ours(args):
         sms = E.device_sm_count(local if ws > 1 else 0)
         max_mhz = (head["clocks"] or {}).get("sm_max_mhz") or 2070.0
         nominal = 2 * 2 * sms * max_mhz * 1e6 / 1e12  # 2 DFMA (4 flops) per SM per cycle at the maximum clock
+        instr_rate = FP64_INSTR_PER_IP * 8 * E_ / (elem_ms * 1e-3)
+        pipe_rate = 2 * sms * max_mhz * 1e6  # FP64 instructions per second the pipe issues
         line["roofline_fp64"] = {"bound": "fp64", "kernel": "k_element", "achieved": ach64, "peak": peak64,
                                  "unit": "TFLOP/s", "frac": ach64 / peak64, "peak_source": "measured (DFMA probe)",
                                  "peak_nominal": nominal, "frac_nominal": ach64 / nominal,
-                                 "flops_per_ip": FP64_FLOPS_PER_IP,
+                                 "flops_per_ip": FP64_FLOPS_PER_IP, "fp64_instructions_per_ip": FP64_INSTR_PER_IP,
+                                 "pipe_instruction_frac": instr_rate / pipe_rate,
                                  "flops_source": "executed DFMA/DADD/DMUL per point, ncu (FMA = 2 flops)"}
     variants = {}
     for prec, r in results.items():

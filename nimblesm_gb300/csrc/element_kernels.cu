@@ -45,13 +45,13 @@ __device__ __forceinline__ void element_work(const ElementArgs& a, const int e);
 template <typename T, bool kPrecomputedGeo, bool kPersistent>
 __global__ void __launch_bounds__(128) k_element(ElementArgs a)
 {
-  if (!kPersistent) {
+  if constexpr (!kPersistent) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e < a.E) element_work<T, kPrecomputedGeo>(a, e);
-    return;
+  } else {
+    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < a.E; e += (long)gridDim.x * blockDim.x)
+      element_work<T, kPrecomputedGeo>(a, (int)e);
   }
-  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < a.E; e += (long)gridDim.x * blockDim.x)
-    element_work<T, kPrecomputedGeo>(a, (int)e);
 }
 
 template <typename T, bool kPrecomputedGeo>
@@ -109,37 +109,42 @@ __device__ __forceinline__ void element_work(const ElementArgs& a, const int e)
 #pragma unroll
   for (int p = 0; p < 8; p++) {
     const int bit[3] = {sx_of(p), sy_of(p), sz_of(p)};
-    T         G0[3][3], W0[3][3];  // J_X^{-1} and det J_X * J_X^{-1}
+    T         G0[3][3], JX[3][3], idet0;  // J_X^{-1}, J_X, 1 / det J_X
     if (kPrecomputedGeo) {
 #pragma unroll
       for (int q = 0; q < 9; q++) {
         G0[q / 3][q % 3] = T(__ldg(&a.geo[(p * kGeoPerPoint + q) * ld_e + e]));
-        W0[q / 3][q % 3] = T(__ldg(&a.geo[(p * kGeoPerPoint + 10 + q) * ld_e + e]));
+        JX[q / 3][q % 3] = T(__ldg(&a.geo[(p * kGeoPerPoint + 10 + q) * ld_e + e]));
       }
+      idet0 = T(__ldg(&a.geo[(p * kGeoPerPoint + 19) * ld_e + e]));
     } else {
-      T JX[3][3], det0;
+      T det0;
 #pragma unroll
       for (int i = 0; i < 3; i++)
 #pragma unroll
         for (int d = 0; d < 3; d++) JX[i][d] = GX[d][i][bit[other1(d)]][bit[other2(d)]];
       invert3<T>(JX, G0, det0);
       if (!(det0 > T(0))) bad = true;  // (checked once at setup in the FP64 form)
-#pragma unroll
-      for (int q = 0; q < 9; q++) W0[q / 3][q % 3] = det0 * G0[q / 3][q % 3];
+      idet0 = reciprocal(det0);
     }
-    // H[i][J] = sum_d du_i/dxi_d G0[d][J]
-    T H[3][3];
+    // Du[i][d] = du_i/dxi_d;  H = Du G0;  J_x = J_X + Du, the current Jacobian
+    T Du[3][3], H[3][3], Jx[3][3];
 #pragma unroll
     for (int i = 0; i < 3; i++)
 #pragma unroll
-      for (int J = 0; J < 3; J++) {
-        T h = T(0);
-#pragma unroll
-        for (int d = 0; d < 3; d++) h += Gu[d][i][bit[other1(d)]][bit[other2(d)]] * G0[d][J];
-        H[i][J] = h;
+      for (int d = 0; d < 3; d++) {
+        Du[i][d] = Gu[d][i][bit[other1(d)]][bit[other2(d)]];
+        Jx[i][d] = JX[i][d] + Du[i][d];
       }
-    T sig[6], C[3][3], J;
-    material_stress<T>(model, H, K, Gm, sig, C, J);
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int J = 0; J < 3; J++) H[i][J] = fma(Du[i][0], G0[0][J], fma(Du[i][1], G0[1][J], Du[i][2] * G0[2][J]));
+    // det J_x = J det J_X, and the force term det(J_x) J_x^{-1} sigma = adj(J_x) sigma
+    T       Cx[3][3];
+    const T J = cofactor3<T>(Jx, Cx) * idet0;
+    T       sig[6];
+    material_stress_j<T>(model, H, J, K, Gm, sig);
     if (!positive(J)) bad = true;  // inverted element
     if (store) {
       T r[kIpRecord];
@@ -152,21 +157,15 @@ __device__ __forceinline__ void element_work(const ElementArgs& a, const int e)
       r[15] = T(0);
       store_vec(rec + (size_t)p * ld_e * kIpRecord, r, kIpRecord);
     }
-    // P = sigma cof(F);  Q[d][i] = sum_J (det J_X J_X^{-1})[d][J] P[i][J],
+    // Q[d][i] = sum_k adj(J_x)[d][k] sigma[k][i] = sum_k cof(J_x)[k][d] sigma[k][i],
     // summed over the two points of each sign pair (the first assigns)
-    T P[3][3];
-#pragma unroll
-    for (int i = 0; i < 3; i++)
-#pragma unroll
-      for (int J = 0; J < 3; J++)
-        P[i][J] = sym(sig, i, 0) * C[0][J] + sym(sig, i, 1) * C[1][J] + sym(sig, i, 2) * C[2][J];
 #pragma unroll
     for (int d = 0; d < 3; d++)
 #pragma unroll
       for (int i = 0; i < 3; i++) {
-        T&      acc = S[d][i][bit[other1(d)]][bit[other2(d)]];
-        const T tail = first_of_pair(d, p) ? W0[d][2] * P[i][2] : fma(W0[d][2], P[i][2], acc);
-        acc          = fma(W0[d][0], P[i][0], fma(W0[d][1], P[i][1], tail));
+        T&      acc  = S[d][i][bit[other1(d)]][bit[other2(d)]];
+        const T tail = first_of_pair(d, p) ? Cx[2][d] * sym(sig, 2, i) : fma(Cx[2][d], sym(sig, 2, i), acc);
+        acc          = fma(Cx[0][d], sym(sig, 0, i), fma(Cx[1][d], sym(sig, 1, i), tail));
       }
   }
 

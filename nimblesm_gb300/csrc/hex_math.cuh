@@ -115,26 +115,27 @@ __device__ __forceinline__ double rcbrt_refined(double J)
 // FP32 form: J^{-1/3} = 2^{-log2(J)/3} with the hardware log2/exp2 (about 2 ulp).
 __device__ __forceinline__ float rcbrt_refined(float J) { return exp2f(__log2f(J) * (-1.0f / 3.0f)); }
 
-// Neo-Hookean Cauchy stress from H = F - I (reference src/nimble_material.cc:252-310):
-// sigma = K/2 (J - 1/J) I + G J^{-5/3} dev(F F^T).  Also returns cof(F) and J.
+// Cofactor matrix of M (C[r][c] = cofactor of entry (r, c)) and det M.
 template <typename T>
-__device__ __forceinline__ void neohookean(const T H[3][3], T K, T G, T sig[6], T C[3][3], T& J)
+__device__ __forceinline__ T cofactor3(const T M[3][3], T C[3][3])
 {
-  T F[3][3];
-#pragma unroll
-  for (int i = 0; i < 3; i++)
-#pragma unroll
-    for (int k = 0; k < 3; k++) F[i][k] = (i == k) ? T(1) + H[i][k] : H[i][k];
-  C[0][0] = F[1][1] * F[2][2] - F[1][2] * F[2][1];
-  C[0][1] = F[1][2] * F[2][0] - F[1][0] * F[2][2];
-  C[0][2] = F[1][0] * F[2][1] - F[1][1] * F[2][0];
-  C[1][0] = F[0][2] * F[2][1] - F[0][1] * F[2][2];
-  C[1][1] = F[0][0] * F[2][2] - F[0][2] * F[2][0];
-  C[1][2] = F[0][1] * F[2][0] - F[0][0] * F[2][1];
-  C[2][0] = F[0][1] * F[1][2] - F[0][2] * F[1][1];
-  C[2][1] = F[0][2] * F[1][0] - F[0][0] * F[1][2];
-  C[2][2] = F[0][0] * F[1][1] - F[0][1] * F[1][0];
-  J       = F[0][0] * C[0][0] + F[0][1] * C[0][1] + F[0][2] * C[0][2];
+  C[0][0] = M[1][1] * M[2][2] - M[1][2] * M[2][1];
+  C[0][1] = M[1][2] * M[2][0] - M[1][0] * M[2][2];
+  C[0][2] = M[1][0] * M[2][1] - M[1][1] * M[2][0];
+  C[1][0] = M[0][2] * M[2][1] - M[0][1] * M[2][2];
+  C[1][1] = M[0][0] * M[2][2] - M[0][2] * M[2][0];
+  C[1][2] = M[0][1] * M[2][0] - M[0][0] * M[2][1];
+  C[2][0] = M[0][1] * M[1][2] - M[0][2] * M[1][1];
+  C[2][1] = M[0][2] * M[1][0] - M[0][0] * M[1][2];
+  C[2][2] = M[0][0] * M[1][1] - M[0][1] * M[1][0];
+  return M[0][0] * C[0][0] + M[0][1] * C[0][1] + M[0][2] * C[0][2];
+}
+
+// Neo-Hookean Cauchy stress (reference src/nimble_material.cc:252-310) from
+// H = F - I and J = det F: sigma = K/2 (J - 1/J) I + G J^{-5/3} dev(F F^T).
+template <typename T>
+__device__ __forceinline__ void neohookean_stress(const T H[3][3], T J, T K, T G, T sig[6])
+{
   // b - I = H + H^T + H H^T, one add and three fused multiply-adds per entry
   T B[6];
 #pragma unroll
@@ -159,29 +160,26 @@ __device__ __forceinline__ void neohookean(const T H[3][3], T K, T G, T sig[6], 
   sig[5]      = Gr5 * B[5];
 }
 
-// Small-strain elastic stress (ElasticMaterial::GetStress,
-// src/nimble_material.cc:98-126): eps = sym(F) - I on the unrotated F,
-// sigma = 2 mu eps + lambda tr(eps) I with lambda = K - 2 mu / 3.  From
-// H = F - I the strain is sym(H), without the cancellation of F_ii - 1.
-// Also returns cof(F) and J = det F for the force and the inversion check.
+// The neo-Hookean stress from H alone; also returns cof(F) and J = det F.
 template <typename T>
-__device__ __forceinline__ void elastic(const T H[3][3], T K, T G, T sig[6], T C[3][3], T& J)
+__device__ __forceinline__ void neohookean(const T H[3][3], T K, T G, T sig[6], T C[3][3], T& J)
 {
   T F[3][3];
 #pragma unroll
   for (int i = 0; i < 3; i++)
 #pragma unroll
     for (int k = 0; k < 3; k++) F[i][k] = (i == k) ? T(1) + H[i][k] : H[i][k];
-  C[0][0] = F[1][1] * F[2][2] - F[1][2] * F[2][1];
-  C[0][1] = F[1][2] * F[2][0] - F[1][0] * F[2][2];
-  C[0][2] = F[1][0] * F[2][1] - F[1][1] * F[2][0];
-  C[1][0] = F[0][2] * F[2][1] - F[0][1] * F[2][2];
-  C[1][1] = F[0][0] * F[2][2] - F[0][2] * F[2][0];
-  C[1][2] = F[0][1] * F[2][0] - F[0][0] * F[2][1];
-  C[2][0] = F[0][1] * F[1][2] - F[0][2] * F[1][1];
-  C[2][1] = F[0][2] * F[1][0] - F[0][0] * F[1][2];
-  C[2][2] = F[0][0] * F[1][1] - F[0][1] * F[1][0];
-  J       = F[0][0] * C[0][0] + F[0][1] * C[0][1] + F[0][2] * C[0][2];
+  J = cofactor3<T>(F, C);
+  neohookean_stress<T>(H, J, K, G, sig);
+}
+
+// Small-strain elastic stress (ElasticMaterial::GetStress,
+// src/nimble_material.cc:98-126): eps = sym(F) - I on the unrotated F,
+// sigma = 2 mu eps + lambda tr(eps) I with lambda = K - 2 mu / 3.  From
+// H = F - I the strain is sym(H), without the cancellation of F_ii - 1.
+template <typename T>
+__device__ __forceinline__ void elastic_stress(const T H[3][3], T K, T G, T sig[6])
+{
   const T two_mu = T(2) * G, lambda = K - T(2) * G / T(3);
   const T tr     = H[0][0] + H[1][1] + H[2][2];
   sig[0]         = two_mu * H[0][0] + lambda * tr;
@@ -192,7 +190,20 @@ __device__ __forceinline__ void elastic(const T H[3][3], T K, T G, T sig[6], T C
   sig[5]         = G * (H[2][0] + H[0][2]);
 }
 
-// The stress of the element's material model.
+// The elastic stress from H alone; also returns cof(F) and J = det F.
+template <typename T>
+__device__ __forceinline__ void elastic(const T H[3][3], T K, T G, T sig[6], T C[3][3], T& J)
+{
+  T F[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int k = 0; k < 3; k++) F[i][k] = (i == k) ? T(1) + H[i][k] : H[i][k];
+  J = cofactor3<T>(F, C);
+  elastic_stress<T>(H, K, G, sig);
+}
+
+// The stress of the element's material model (also cof(F) and J).
 template <typename T>
 __device__ __forceinline__ void material_stress(int model, const T H[3][3], T K, T G, T sig[6], T C[3][3], T& J)
 {
@@ -200,6 +211,16 @@ __device__ __forceinline__ void material_stress(int model, const T H[3][3], T K,
     elastic<T>(H, K, G, sig, C, J);
   else
     neohookean<T>(H, K, G, sig, C, J);
+}
+
+// The stress of the element's material model from H and J = det F.
+template <typename T>
+__device__ __forceinline__ void material_stress_j(int model, const T H[3][3], T J, T K, T G, T sig[6])
+{
+  if (model == kElastic)
+    elastic_stress<T>(H, K, G, sig);
+  else
+    neohookean_stress<T>(H, J, K, G, sig);
 }
 
 template <typename T>

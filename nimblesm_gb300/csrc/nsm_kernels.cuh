@@ -21,9 +21,9 @@ struct GroupMaterial {
 };
 
 // Reference geometry per integration point (FP64 form), planes
-// [8 * kGeoPerPoint][ld_e]: per point J_X^{-1} (9, row-major), det J_X, and
-// det J_X * J_X^{-1} (9), the factor of the point's force term.
-constexpr int kGeoPerPoint = 19;
+// [8 * kGeoPerPoint][ld_e]: per point J_X^{-1} (9, row-major), det J_X,
+// J_X = dX/dxi (9, row-major) and 1 / det J_X.
+constexpr int kGeoPerPoint = 20;
 
 struct SetupArgs {
   int           N, E;

@@ -105,9 +105,10 @@ __global__ void k_setup_elements(int E, long ld_e, const int* __restrict__ conn,
     for (int k = 0; k < 3; k++)
       for (int J = 0; J < 3; J++) {
         geo[(ip * kGeoPerPoint + k * 3 + J) * ld_e + e]      = bi[k][J];
-        geo[(ip * kGeoPerPoint + 10 + k * 3 + J) * ld_e + e] = det * bi[k][J];
+        geo[(ip * kGeoPerPoint + 10 + k * 3 + J) * ld_e + e] = b[k][J];
       }
-    geo[(ip * kGeoPerPoint + 9) * ld_e + e] = det;
+    geo[(ip * kGeoPerPoint + 9) * ld_e + e]  = det;
+    geo[(ip * kGeoPerPoint + 19) * ld_e + e] = 1.0 / det;
   }
   for (int i = 0; i < 8; i++) {
     double m = 0.0;

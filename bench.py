@@ -119,6 +119,12 @@ def dist_env():
     return ws, rank, local
 
 
+def replica_value(units_per_rank, ms_per_rank, reps):
+    """Whole-job throughput of weak-scaled replicas: the units all ranks
+    processed over the slowest rank's time (ms)."""
+    return reps.sum(units_per_rank) / (reps.max(ms_per_rank) * 1e-3)
+
+
 def cpu_baseline(problem, dt, seconds_budget=15.0, threads=None, max_steps=40):
     """The oracle (C restatement of the reference's host path, whose gather
     assembly is the reference's serial order at any thread count) on all host
@@ -327,15 +333,10 @@ def accuracy_variant(E, args, problem, device, mlp):
 def run_ours(args):
     from nimblesm_gb300 import engine as E
 
-    ws, rank, local = dist_env()
-    dist = None
-    if ws > 1:
-        import torch
-        import torch.distributed as tdist
+    from nimblesm_gb300.replicas import Replicas
 
-        torch.cuda.set_device(local)
-        tdist.init_process_group("nccl")
-        dist = (torch, tdist)
+    reps = Replicas()
+    ws, rank, local = reps.world, reps.rank, reps.device
 
     n = args.n
     problem = cube_problem(n, jitter=0.2, seed=0)
@@ -346,30 +347,21 @@ def run_ours(args):
     sched = max(SCHEDULE_STEPS, args.warmup + 2 * args.steps + 1)
     final_time = sched * dt
 
-    def barrier():
-        if dist:
-            dist[1].barrier()
-            dist[0].cuda.synchronize()
-
-    def max_over_ranks(x):
-        if not dist:
-            return x
-        t = dist[0].tensor([x], dtype=dist[0].float64, device="cuda")
-        dist[1].all_reduce(t, op=dist[1].ReduceOp.MAX)
-        return float(t.item())
+    barrier, max_over_ranks = reps.barrier, reps.max
 
     results = {}
     for precision in ([args.precision] + ([p for p in ("fp64", "fp32") if p != args.precision]
                                           if args.variants else [])):
-        m = E.Model(problem, precision=precision, device=local if ws > 1 else 0)
+        m = E.Model(problem, precision=precision, device=local)
         m.begin(final_time, sched, sched)
         m.advance(args.warmup)
         m.synchronize()
         barrier()
         with ClockSampler(local) as clk:
-            ms = m.advance_timed(args.steps)
+            ms_rank = m.advance_timed(args.steps)
         barrier()
-        ms = max_over_ranks(ms)
+        value_p = replica_value(8.0 * E_ * args.steps, ms_rank, reps)
+        ms = max_over_ranks(ms_rank)
         # per-kernel device times over the same number of steps (events on the
         # engine's stream around every element and node launch)
         m.set_profiling(True)
@@ -377,15 +369,15 @@ def run_ours(args):
         prof = m.get_profile()
         m.set_profiling(False)
         state_u = m.GetVectorNodeData("displacement")
-        results[precision] = dict(ms=ms, prof=prof, clocks=clk.summary(), launches=m.launches_per_advance(args.steps),
-                                  u=state_u, model=m)
+        results[precision] = dict(ms=ms, value=value_p, prof=prof, clocks=clk.summary(),
+                                  launches=m.launches_per_advance(args.steps), u=state_u, model=m)
         if precision != args.precision:
             m.close()
 
     head = results[args.precision]
     m = head["model"]
     ms = head["ms"]
-    value = 8.0 * E_ * args.steps * ws / (ms * 1e-3)
+    value = head["value"]
 
     # end to end through the drop-in host-buffer entry point: each step copies
     # the displacement in from pinned host memory and the internal force out
@@ -400,8 +392,7 @@ def run_ours(args):
         m.ComputeInternalForceHost(u_host.array, f_host.array)
     t1 = time.perf_counter()
     barrier()
-    e2e_s = max_over_ranks(t1 - t0)
-    e2e_value = 8.0 * E_ * e2e_steps * ws / e2e_s
+    e2e_value = replica_value(8.0 * E_ * e2e_steps, 1e3 * (t1 - t0), reps)
 
     step_bytes, elem_bytes = algorithmic_bytes(N, E_, args.precision)
     peak, peak_kind = hbm_peak()
@@ -428,9 +419,9 @@ def run_ours(args):
     }
     if args.precision == "fp64":
         # the roof that binds the FP64 element kernel: the FP64 pipe
-        peak64 = E.fp64_peak_tflops(local if ws > 1 else 0)
+        peak64 = E.fp64_peak_tflops(local)
         ach64 = FP64_FLOPS_PER_IP * 8 * E_ / (elem_ms * 1e-3) / 1e12
-        sms = E.device_sm_count(local if ws > 1 else 0)
+        sms = E.device_sm_count(local)
         max_mhz = (head["clocks"] or {}).get("sm_max_mhz") or 2070.0
         nominal = 2 * 2 * sms * max_mhz * 1e6 / 1e12  # 2 DFMA (4 flops) per SM per cycle at the maximum clock
         instr_rate = FP64_INSTR_PER_IP * 8 * E_ / (elem_ms * 1e-3)
@@ -445,23 +436,23 @@ def run_ours(args):
     for prec, r in results.items():
         if prec == args.precision:
             continue
-        v = 8.0 * E_ * args.steps * ws / (r["ms"] * 1e-3)
+        v = r["value"]
         err = float(np.linalg.norm(r["u"] - head["u"]) / max(np.linalg.norm(head["u"]), 1e-300))
         variants[prec] = {"value": v, "ms_per_step": r["ms"] / args.steps, "speedup_vs_fp64": v / value,
                           "rel_disp_err_vs_fp64": err, "after_steps": args.warmup + args.steps,
                           "element_launch_ms": r["prof"]["element_ms"] / max(r["prof"]["element_launches"], 1),
                           "clocks": r["clocks"]}
     if args.variants and args.uq_steps > 0:
-        variants.update(uq_variants(E, args, local if ws > 1 else 0))
+        variants.update(uq_variants(E, args, local))
     if args.variants and args.big_steps > 0:
-        variants.update(big_fp32_variant(E, args, local if ws > 1 else 0))
+        variants.update(big_fp32_variant(E, args, local))
     mlp = None
     if args.variants and args.mlp_steps > 0:
         fp32_value = variants.get("fp32", {}).get("value", float("nan"))
-        res, mlp = mlp_variant(E, args, problem, local if ws > 1 else 0, value / ws, fp32_value / ws)
+        res, mlp = mlp_variant(E, args, problem, local, value / ws, fp32_value / ws)
         variants.update(res)
     if args.variants and args.acc_steps > 0:
-        variants.update(accuracy_variant(E, args, problem, local if ws > 1 else 0, mlp))
+        variants.update(accuracy_variant(E, args, problem, local, mlp))
     if mlp is not None:
         mlp.close()
     if variants:
@@ -472,8 +463,7 @@ def run_ours(args):
     m.close()
     if rank == 0:
         print(json.dumps(line), flush=True)
-    if dist:
-        dist[1].destroy_process_group()
+    reps.close()
     return 0
 
 

@@ -244,6 +244,14 @@ int nsm_time_kernels(nsm_model* model, int repeats, double* element_ms, double* 
  * launches of each candidate on this model; returns the chosen candidate and
  * its mean time in milliseconds.  Captured graphs are rebuilt. */
 int nsm_autotune(nsm_model* model, int repeats, int* chosen, double* best_ms);
+/* The autotuner's measurements: mean milliseconds of `repeats` element-kernel
+ * launches for each candidate launch shape, in candidate order, into
+ * ms[0 .. capacity); *count receives the number of candidates.  The model's
+ * own launch shape is left as it was. */
+int nsm_launch_candidate_times(nsm_model* model, int repeats, double* ms, int capacity, int* count);
+/* Sets the element kernel's launch shape to candidate `candidate` of the
+ * autotuner's list (what nsm_autotune does with its choice). */
+int nsm_set_launch_candidate(nsm_model* model, int candidate);
 /* Number of kernel launches nsm_advance(model, num_steps) issues. */
 int nsm_launches_per_advance(nsm_model* model, int num_steps);
 /* Profiling mode: nsm_advance launches without CUDA graphs and brackets each

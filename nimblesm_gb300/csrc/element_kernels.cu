@@ -35,33 +35,125 @@ __device__ __forceinline__ double load_node<double>(const double* f64, const flo
 template <>
 __device__ __forceinline__ float load_node<float>(const double*, const float* f32, long i) { return __ldg(&f32[i]); }
 
+// Where an element's nodal values come from.  GlobalNodes: gathered from the
+// node planes through the connectivity.  StagedNodes: this thread's slots of a
+// shared-memory stage that cp.async filled one element ahead (FP32 form).
+template <typename T>
+struct GlobalNodes {
+  const ElementArgs& a;
+  int                id[8];
+  __device__ __forceinline__ GlobalNodes(const ElementArgs& args, int e) : a(args)
+  {
+#pragma unroll
+    for (int n = 0; n < 8; n++) id[n] = __ldg(&a.conn[n * a.ld_e + e]);
+  }
+  __device__ __forceinline__ T u(int n, int k) const { return load_node<T>(a.u, a.uf, k * a.ld_n + id[n]); }
+  __device__ __forceinline__ T X(int n, int k) const { return __ldg(&a.Xf[k * a.ld_n + id[n]]); }
+};
+
+// Stage layout: [48][blockDim] floats per element slot, values 0..23 u
+// (node-major, 3 components), 24..47 X; thread t owns column t, so the lanes of
+// a warp read consecutive words.
+constexpr int kStageValues = 48;
+struct StagedNodes {
+  const float* s;  // this thread's column of the stage
+  int          B;  // column stride (threads per block)
+  __device__ __forceinline__ float u(int n, int k) const { return s[(n * 3 + k) * B]; }
+  __device__ __forceinline__ float X(int n, int k) const { return s[(24 + n * 3 + k) * B]; }
+};
+
 // FP64 form: reference geometry precomputed (geo planes).  FP32 form: the
 // reference Jacobian is rebuilt from X each step with the same transform.
-template <typename T, bool kPrecomputedGeo>
-__device__ __forceinline__ void element_work(const ElementArgs& a, const int e);
+template <typename T, bool kPrecomputedGeo, class Nodes>
+__device__ __forceinline__ void element_work(const ElementArgs& a, const int e, const Nodes& nodes);
 
 // One thread per element, or (persistent form) a fixed grid of blocks walking
 // the elements of all samples in tiles of blockDim.x.
-template <typename T, bool kPrecomputedGeo, bool kPersistent>
-__global__ void __launch_bounds__(128) k_element(ElementArgs a)
+template <typename T, bool kPrecomputedGeo, bool kPersistent, int kMinBlocks = 1>
+__global__ void __launch_bounds__(128, kMinBlocks) k_element(ElementArgs a)
 {
   if constexpr (!kPersistent) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e < a.E) element_work<T, kPrecomputedGeo>(a, e);
+    if (e < a.E) element_work<T, kPrecomputedGeo>(a, e, GlobalNodes<T>(a, e));
   } else {
     for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < a.E; e += (long)gridDim.x * blockDim.x)
-      element_work<T, kPrecomputedGeo>(a, (int)e);
+      element_work<T, kPrecomputedGeo>(a, (int)e, GlobalNodes<T>(a, (int)e));
   }
 }
 
-template <typename T, bool kPrecomputedGeo>
-__device__ __forceinline__ void element_work(const ElementArgs& a, const int e)
+// Staged FP32 form: a persistent grid in which each thread walks the elements
+// e, e + stride, ... with the next element's 48 nodal values (u and X) and the
+// connectivity of the one after in flight as cp.async copies into its own
+// shared-memory columns while it computes the current element.  Neither the
+// connectivity load nor the gather it addresses stalls the element math, and
+// nothing staged is held in registers.  Copy groups are per thread and each
+// thread reads only its own columns: no block barrier is needed.
+__device__ __forceinline__ void cp_async4(void* dst, const void* src)
 {
-  const long ld_e = a.ld_e, ld_n = a.ld_n;
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
-  int id[8];
+// Per thread and slot: kStageValues floats (values 0..23 u, 24..47 X), then
+// 8 connectivity entries; column stride B.  Two slots, for the element being
+// computed and the next one.
+constexpr int kStageWords = kStageValues + 8;
+
+__device__ __forceinline__ void stage_conn(const ElementArgs& a, long e, int* col, int B)
+{
 #pragma unroll
-  for (int n = 0; n < 8; n++) id[n] = __ldg(&a.conn[n * ld_e + e]);
+  for (int n = 0; n < 8; n++) cp_async4(col + n * B, a.conn + n * a.ld_e + e);
+}
+
+__device__ __forceinline__ void stage_nodes(const ElementArgs& a, const int* conn_col, float* col, int B)
+{
+#pragma unroll
+  for (int n = 0; n < 8; n++) {
+    const int id = conn_col[n * B];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      cp_async4(col + (n * 3 + k) * B, a.uf + k * a.ld_n + id);
+      cp_async4(col + (24 + n * 3 + k) * B, a.Xf + k * a.ld_n + id);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(128, 3) k_element_staged(ElementArgs a)
+{
+  extern __shared__ float stage_mem[];  // [2][kStageWords][blockDim.x]
+  const int  B      = blockDim.x;
+  const long stride = (long)gridDim.x * B;
+  const int  slot   = kStageWords * B;
+  float*     cur    = stage_mem + threadIdx.x;  // slot of the element being computed
+  float*     nxt    = cur + slot;               // slot of the next one
+  long       e      = blockIdx.x * (long)B + threadIdx.x;
+  // prologue: connectivity of e (waited for), its nodal values and the
+  // connectivity of e + stride in flight
+  if (e < a.E) stage_conn(a, e, reinterpret_cast<int*>(cur + kStageValues * B), B);
+  cp_async_commit();
+  cp_async_wait_all();
+  if (e < a.E) stage_nodes(a, reinterpret_cast<const int*>(cur + kStageValues * B), cur, B);
+  if (e + stride < a.E) stage_conn(a, e + stride, reinterpret_cast<int*>(nxt + kStageValues * B), B);
+  cp_async_commit();
+  for (; e < a.E; e += stride) {
+    cp_async_wait_all();  // this element's values and the next one's connectivity
+    if (e + stride < a.E) stage_nodes(a, reinterpret_cast<const int*>(nxt + kStageValues * B), nxt, B);
+    if (e + 2 * stride < a.E) stage_conn(a, e + 2 * stride, reinterpret_cast<int*>(cur + kStageValues * B), B);
+    cp_async_commit();
+    element_work<float, false>(a, (int)e, StagedNodes{cur, B});
+    float* t = cur;
+    cur      = nxt;
+    nxt      = t;
+  }
+  cp_async_wait_all();
+}
+
+template <typename T, bool kPrecomputedGeo, class Nodes>
+__device__ __forceinline__ void element_work(const ElementArgs& a, const int e, const Nodes& nodes)
+{
+  const long ld_e = a.ld_e;
 
   // displacement gradient at the points (36 distinct values)
   T Gu[3][3][2][2];
@@ -70,16 +162,16 @@ __device__ __forceinline__ void element_work(const ElementArgs& a, const int e)
 #pragma unroll
     for (int n = 0; n < 8; n++)
 #pragma unroll
-      for (int k = 0; k < 3; k++) x[n][k] = load_node<T>(a.u, a.uf, k * ld_n + id[n]);
+      for (int k = 0; k < 3; k++) x[n][k] = nodes.u(n, k);
     nodal_gradient<T>(x, Gu);
   }
   T GX[3][3][2][2];
-  if (!kPrecomputedGeo) {
+  if constexpr (!kPrecomputedGeo) {
     T x[8][3];
 #pragma unroll
     for (int n = 0; n < 8; n++)
 #pragma unroll
-      for (int k = 0; k < 3; k++) x[n][k] = __ldg(&a.Xf[k * ld_n + id[n]]);
+      for (int k = 0; k < 3; k++) x[n][k] = nodes.X(n, k);
     nodal_gradient<T>(x, GX);
   }
 
@@ -109,7 +201,7 @@ __device__ __forceinline__ void element_work(const ElementArgs& a, const int e)
 #pragma unroll
   for (int p = 0; p < 8; p++) {
     const int bit[3] = {sx_of(p), sy_of(p), sz_of(p)};
-    T         G0[3][3], JX[3][3], idet0;  // J_X^{-1}, J_X, 1 / det J_X
+    T         G0[3][3], JX[3][3], idet0;  // J_X^{-1} / 8, 8 J_X, 1 / (512 det J_X)
     if (kPrecomputedGeo) {
 #pragma unroll
       for (int q = 0; q < 9; q++) {
@@ -127,7 +219,7 @@ __device__ __forceinline__ void element_work(const ElementArgs& a, const int e)
       if (!(det0 > T(0))) bad = true;  // (checked once at setup in the FP64 form)
       idet0 = reciprocal(det0);
     }
-    // Du[i][d] = du_i/dxi_d;  H = Du G0;  J_x = J_X + Du, the current Jacobian
+    // Du[i][d] = 8 du_i/dxi_d;  H = Du G0;  8 J_x = 8 J_X + Du, J_x the current Jacobian
     T Du[3][3], H[3][3], Jx[3][3];
 #pragma unroll
     for (int i = 0; i < 3; i++)
@@ -169,26 +261,10 @@ __device__ __forceinline__ void element_work(const ElementArgs& a, const int e)
       }
   }
 
-  // f_a,i = - sum_p sum_d dN_a/dxi_d(p) Q_p[d][i]  (direction 0 assigns)
+  // f_a,i = - sum_p sum_d dN_a/dxi_d(p) Q_p[d][i].  J_x and hence Q carry
+  // the factor 8^2 of the modal gradient, dN/dxi another 8: scale -1/512.
   T f[8][3];
-#pragma unroll
-  for (int d = 0; d < 3; d++) {
-    const int o1 = other1(d), o2 = other2(d);
-#pragma unroll
-    for (int i = 0; i < 3; i++) {
-      T R[2][2];
-      bwd_transform<T>(S[d][i], R);
-#pragma unroll
-      for (int b = 0; b < 2; b++)
-#pragma unroll
-        for (int c = 0; c < 2; c++) {
-          T& hi = f[corner_axes(d, 1, o1, b, o2, c)][i];
-          T& lo = f[corner_axes(d, 0, o1, b, o2, c)][i];
-          hi    = d == 0 ? -R[b][c] : hi - R[b][c];
-          lo    = d == 0 ? R[b][c] : lo + R[b][c];
-        }
-    }
-  }
+  nodal_adjoint<T>(S, T(-1.0 / 512.0), f);
   T    fv[24];
   bool finite = true;
 #pragma unroll
@@ -249,10 +325,15 @@ static cudaError_t launch_element(ElementArgs a, const ElementLaunch& l, cudaStr
     int g = l.blocks_per_sm * num_sms();
     if (g < grid) grid = g;
   }
+  // register bound: FP32 for 3 blocks of 128 per SM (measured fastest); FP64
+  // none, or 3 blocks
+  constexpr int kMin = sizeof(T) == 4 ? 3 : 1;
   if (l.persistent)
-    k_element<T, kGeo, true><<<grid, block, 0, stream>>>(a);
+    k_element<T, kGeo, true, kMin><<<grid, block, 0, stream>>>(a);
+  else if (l.blocks_per_sm == 3 && block == 128)
+    k_element<T, kGeo, false, 3><<<grid, block, 0, stream>>>(a);
   else
-    k_element<T, kGeo, false><<<grid, block, 0, stream>>>(a);
+    k_element<T, kGeo, false, kMin><<<grid, block, 0, stream>>>(a);
   return cudaGetLastError();
 }
 
@@ -263,7 +344,27 @@ cudaError_t launch_element_fp64(const ElementArgs& a, const ElementLaunch& l, cu
 
 cudaError_t launch_element_fp32(const ElementArgs& a, const ElementLaunch& l, cudaStream_t stream)
 {
-  return launch_element<float, false>(a, l, stream);
+  if (!l.staged) return launch_element<float, false>(a, l, stream);
+  if (a.E == 0) return cudaSuccess;
+  const int    block = (l.block == 64 || l.block == 128) ? l.block : 128;
+  const size_t smem  = 2 * kStageWords * block * sizeof(float);
+  static bool  configured = false;
+  if (!configured) {  // 56 KB at 128 threads: above the default 48 KB of dynamic shared memory
+    const int   most = 2 * kStageWords * 128 * (int)sizeof(float);
+    cudaError_t err  = cudaSuccess;
+    err = cudaFuncSetAttribute(k_element_staged, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
+    if (err == cudaSuccess)
+      err = cudaFuncSetAttribute(k_element_staged, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    if (err != cudaSuccess) return err;
+    configured = true;
+  }
+  ElementArgs  b     = a;
+  b.persistent       = 1;
+  int grid           = grid_for(a.E, block);
+  const int g        = (l.blocks_per_sm > 0 ? l.blocks_per_sm : 1) * num_sms();
+  if (g < grid) grid = g;
+  k_element_staged<<<grid, block, smem, stream>>>(b);
+  return cudaGetLastError();
 }
 
 // Energies of the current state, FP64 whatever the element precision:

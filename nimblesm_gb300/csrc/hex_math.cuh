@@ -8,68 +8,171 @@
 // f_a = -sum_ip (dN_a/dx . sigma) det(dx/dxi) w (src/nimble_element.h:540-625).
 // How it is computed is chosen to spend as few FP64 operations as possible
 // (FP64 is this chip's narrow pipe, ~1.2 TFLOP/s):
-//   * Tensor-product structure of the trilinear hex: du/dxi at the 8 points
-//     takes only 4 distinct values (it does not depend on xi), formed from the
-//     4 edge differences along xi by two 2-point transforms; same for eta and
+//   * Modal (tensor-product) form of the trilinear hex: du/dxi at the 8
+//     points takes only 4 distinct values (it does not depend on xi), formed
+//     from the Hadamard transform of the corner values; same for eta and
 //     zeta.  36 values replace the 72 sums of 8 products per point.  The
-//     force assembly (transpose of the gradient) uses the same transform.
-//   * H = F - I = (du/dxi) J_X^{-1}, with J_X^{-1} and det J_X precomputed
-//     per point at setup; no cancellation in F - I, no per-step inverse.
-//   * sigma from b - I = H + H^T + H H^T and J = det F through the cofactor
-//     matrix (no polar decomposition: the reference's V V equals F F^T).
+//     force assembly is the transpose: signed point sums to modal
+//     coefficients, then the inverse transform to the corners.
+//   * H = F - I = (du/dxi) J_X^{-1}, with J_X^{-1}, J_X and 1/det J_X
+//     precomputed per point at setup; no cancellation in F - I, no per-step
+//     inverse.
+//   * sigma from b - I = H + H^T + H H^T and J = det J_x / det J_X through the
+//     cofactors of the current Jacobian J_x = J_X + du/dxi (no polar
+//     decomposition: the reference's V V equals F F^T).
 //   * J^{-1/3} from an FP32 seed and one third-order correction, so that
 //     1/J = r^3 and J^{-5/3} = r^5 need no division.
-//   * Forces from the first Piola-Kirchhoff form P = sigma cof(F), since
-//     det(J_x) J_x^{-1} sigma = det(J_X) J_X^{-1} P^T.
+//   * Forces from det(J_x) J_x^{-1} sigma = adj(J_x) sigma, the adjugate
+//     being the transposed cofactor matrix already formed for J.
 #pragma once
 
 #include "nsm_common.cuh"
 
 namespace nsm {
 
+// Weights of the one-axis form (1 +- g) / 8 of the shape-function
+// derivatives at the Gauss points; the fused closure kernel evaluates its
+// gradient with them.
 template <typename T>
 struct Weights {
-  // w(+) = 1 + g, w(-) = 1 - g; the 1/8 of the shape functions is folded into c1, c2.
   static constexpr T wp = T(1.0 + kGauss);
   static constexpr T wm = T(1.0 - kGauss);
   static constexpr T c1 = T((1.0 + kGauss) / 8.0);
   static constexpr T c2 = T((1.0 - kGauss) / 8.0);
 };
 
-// Edge differences D[b][c] (b, c = sign bits along the two other axes) ->
-// derivative values at the Gauss-point sign pairs out[s][t].
+// Modal form of the trilinear hex.  With corner signs s_c = +-1 per axis,
+//   x(xi) = 1/8 sum_m A_m prod_{axes k in m} xi_k,   A_m = sum_c x_c prod_{k in m} s_{c,k},
+// over the 8 axis subsets m (bit k of m set = axis k in m); A is the
+// Hadamard transform of the corner values.  dx/dxi_d at a Gauss point with
+// coordinates sigma_1 g, sigma_2 g along the other two axes is then
+//   1/8 (A_d + g (sigma_1 A_{d,o1} + sigma_2 A_{d,o2}) + g^2 sigma_1 sigma_2 A_{d,o1,o2}),
+// which takes 4 distinct values per direction.  The functions below work
+// with 8 x dx/dxi (the 1/8 is a power of two, folded exactly into the stored
+// reference geometry: J_X^{-1} / 8, 8 J_X, 1 / (512 det J_X)).
 template <typename T>
-__device__ __forceinline__ void fwd_transform(const T D[2][2], T out[2][2])
+__device__ __forceinline__ T& mode(T A[2][2][2], int m)
 {
-  using W = Weights<T>;
-  T E[2][2];  // E[c][s]
+  return A[m & 1][(m >> 1) & 1][(m >> 2) & 1];
+}
+
+// A_m of component i of x[8][3] for every m but the constant mode: three
+// stages of butterflies (23 additions).
+template <typename T>
+__device__ __forceinline__ void modal_coefficients(const T x[8][3], int i, T A[2][2][2])
+{
+  T P[2][2][2];  // after the xi stage: P[mx][by][bz]
 #pragma unroll
-  for (int c = 0; c < 2; c++) {
-    E[c][1] = W::wp * D[1][c] + W::wm * D[0][c];
-    E[c][0] = W::wm * D[1][c] + W::wp * D[0][c];
-  }
+  for (int by = 0; by < 2; by++)
 #pragma unroll
-  for (int s = 0; s < 2; s++) {
-    out[s][1] = W::c1 * E[1][s] + W::c2 * E[0][s];
-    out[s][0] = W::c2 * E[1][s] + W::c1 * E[0][s];
+    for (int bz = 0; bz < 2; bz++) {
+      const T hi = x[corner_of(1, by, bz)][i], lo = x[corner_of(0, by, bz)][i];
+      P[0][by][bz] = hi + lo;
+      P[1][by][bz] = hi - lo;
+    }
+  T Q[2][2][2];  // after the eta stage: Q[mx][my][bz]
+#pragma unroll
+  for (int mx = 0; mx < 2; mx++)
+#pragma unroll
+    for (int bz = 0; bz < 2; bz++) {
+      Q[mx][0][bz] = P[mx][1][bz] + P[mx][0][bz];
+      Q[mx][1][bz] = P[mx][1][bz] - P[mx][0][bz];
+    }
+#pragma unroll
+  for (int mx = 0; mx < 2; mx++)
+#pragma unroll
+    for (int my = 0; my < 2; my++) {
+      A[mx][my][0] = (mx | my) ? Q[mx][my][1] + Q[mx][my][0] : T(0);  // the constant mode is not needed
+      A[mx][my][1] = Q[mx][my][1] - Q[mx][my][0];
+    }
+}
+
+// Gradient values of a nodal field x[8][3]: G[d][i][s][t] = 8 dx_i/dxi_d at
+// the points whose sign bits along the other axes of d are (s, t).
+template <typename T>
+__device__ __forceinline__ void nodal_gradient(const T x[8][3], T G[3][3][2][2])
+{
+  constexpr T g = T(kGauss), g2 = T(kGauss * kGauss);
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    T A[2][2][2];
+    modal_coefficients<T>(x, i, A);
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+      const int o1 = other1(d), o2 = other2(d);
+      const T   a  = mode(A, 1 << d);
+      const T   b1 = mode(A, (1 << d) | (1 << o1)), b2 = mode(A, (1 << d) | (1 << o2));
+      const T   c  = mode(A, 7);
+      const T   same = fma(g2, c, a), diff = fma(-g2, c, a);  // sigma_1 sigma_2 = +1 / -1
+      const T   P = b1 + b2, M = b1 - b2;
+      G[d][i][1][1] = fma(g, P, same);
+      G[d][i][0][0] = fma(-g, P, same);
+      G[d][i][1][0] = fma(g, M, diff);
+      G[d][i][0][1] = fma(-g, M, diff);
+    }
   }
 }
 
-// Adjoint of fwd_transform: sums at sign pairs S[s][t] -> edge values R[b][c].
+// Transpose of nodal_gradient, times `scale`: f[c][i] = scale sum_d sum_{s,t}
+// (8 dN_c/dxi_d)(s, t) S[d][i][s][t].  The point sums are taken to modal
+// coefficients B_m (4 signed sums per direction), which one inverse
+// Hadamard transform (butterflies) takes to the corners.
 template <typename T>
-__device__ __forceinline__ void bwd_transform(const T S[2][2], T R[2][2])
+__device__ __forceinline__ void nodal_adjoint(const T S[3][3][2][2], T scale, T f[8][3])
 {
-  using W = Weights<T>;
-  T Z[2][2];  // Z[s][c]
+  const T k1 = scale * T(kGauss), k2 = scale * T(kGauss * kGauss);
 #pragma unroll
-  for (int s = 0; s < 2; s++) {
-    Z[s][1] = W::c1 * S[s][1] + W::c2 * S[s][0];
-    Z[s][0] = W::c2 * S[s][1] + W::c1 * S[s][0];
-  }
+  for (int i = 0; i < 3; i++) {
+    T T0[3], T1[3], T2[3], T12[3];  // sum S, sum sigma_1 S, sum sigma_2 S, sum sigma_1 sigma_2 S
 #pragma unroll
-  for (int c = 0; c < 2; c++) {
-    R[1][c] = W::wp * Z[1][c] + W::wm * Z[0][c];
-    R[0][c] = W::wm * Z[1][c] + W::wp * Z[0][c];
+    for (int d = 0; d < 3; d++) {
+      const T(&v)[2][2] = S[d][i];
+      const T up = v[1][1] + v[0][0], um = v[1][1] - v[0][0];
+      const T wp = v[1][0] + v[0][1], wm = v[1][0] - v[0][1];
+      T0[d] = up + wp;
+      T12[d] = up - wp;
+      T1[d] = um + wm;
+      T2[d] = um - wm;
+    }
+    // B_m: direction d contributes to {d} (T0), {d, o1} (T1), {d, o2} (T2)
+    // and {x, y, z} (T12); other1/other2 of x are y, z; of y, x, z; of z, x, y.
+    T B[2][2][2];
+    mode(B, 1) = scale * T0[0];
+    mode(B, 2) = scale * T0[1];
+    mode(B, 4) = scale * T0[2];
+    mode(B, 3) = k1 * (T1[0] + T1[1]);
+    mode(B, 5) = k1 * (T2[0] + T1[2]);
+    mode(B, 6) = k1 * (T2[1] + T2[2]);
+    mode(B, 7) = k2 * (T12[0] + T12[1] + T12[2]);
+    // inverse transform: zeta stage (the constant mode is zero), eta, xi
+    T R[2][2][2];  // R[mx][my][bz]
+#pragma unroll
+    for (int mx = 0; mx < 2; mx++)
+#pragma unroll
+      for (int my = 0; my < 2; my++) {
+        if (mx | my) {
+          R[mx][my][1] = B[mx][my][0] + B[mx][my][1];
+          R[mx][my][0] = B[mx][my][0] - B[mx][my][1];
+        } else {
+          R[0][0][1] = B[0][0][1];
+          R[0][0][0] = -B[0][0][1];
+        }
+      }
+    T U[2][2][2];  // U[mx][by][bz]
+#pragma unroll
+    for (int mx = 0; mx < 2; mx++)
+#pragma unroll
+      for (int bz = 0; bz < 2; bz++) {
+        U[mx][1][bz] = R[mx][0][bz] + R[mx][1][bz];
+        U[mx][0][bz] = R[mx][0][bz] - R[mx][1][bz];
+      }
+#pragma unroll
+    for (int by = 0; by < 2; by++)
+#pragma unroll
+      for (int bz = 0; bz < 2; bz++) {
+        f[corner_of(1, by, bz)][i] = U[0][by][bz] + U[1][by][bz];
+        f[corner_of(0, by, bz)][i] = U[0][by][bz] - U[1][by][bz];
+      }
   }
 }
 
@@ -80,27 +183,6 @@ __host__ __device__ constexpr bool first_of_pair(int d, int p)
 {
   return p < corner_of(d == 0 ? 1 - sx_of(p) : sx_of(p), d == 1 ? 1 - sy_of(p) : sy_of(p),
                        d == 2 ? 1 - sz_of(p) : sz_of(p));
-}
-
-// Gradient values of a nodal field x[8][3]: G[d][i][s][t] = dx_i/dxi_d at the
-// points whose sign bits along the other axes of d are (s, t).
-template <typename T>
-__device__ __forceinline__ void nodal_gradient(const T x[8][3], T G[3][3][2][2])
-{
-#pragma unroll
-  for (int d = 0; d < 3; d++) {
-    const int o1 = other1(d), o2 = other2(d);
-#pragma unroll
-    for (int i = 0; i < 3; i++) {
-      T D[2][2];
-#pragma unroll
-      for (int b = 0; b < 2; b++)
-#pragma unroll
-        for (int c = 0; c < 2; c++)
-          D[b][c] = x[corner_axes(d, 1, o1, b, o2, c)][i] - x[corner_axes(d, 0, o1, b, o2, c)][i];
-      fwd_transform<T>(D, G[d][i]);
-    }
-  }
 }
 
 __device__ __forceinline__ double rcbrt_refined(double J)

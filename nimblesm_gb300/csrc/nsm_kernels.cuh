@@ -21,8 +21,9 @@ struct GroupMaterial {
 };
 
 // Reference geometry per integration point (FP64 form), planes
-// [8 * kGeoPerPoint][ld_e]: per point J_X^{-1} (9, row-major), det J_X,
-// J_X = dX/dxi (9, row-major) and 1 / det J_X.
+// [8 * kGeoPerPoint][ld_e]: per point J_X^{-1} / 8 (9, row-major), det J_X,
+// 8 J_X = 8 dX/dxi (9, row-major) and 1 / (512 det J_X).  The factors are
+// those of the modal gradient (8 du/dxi); powers of two, so exact.
 constexpr int kGeoPerPoint = 20;
 
 struct SetupArgs {
@@ -92,6 +93,7 @@ struct ElementLaunch {
   int block;        // threads per block
   int persistent;   // 0: one thread per element, 1: grid-stride with `waves` blocks per SM
   int blocks_per_sm;
+  int staged;       // FP32 form: persistent, nodal values staged one element ahead by cp.async
 };
 cudaError_t launch_element_fp64(const ElementArgs& a, const ElementLaunch& l, cudaStream_t stream);
 cudaError_t launch_element_fp32(const ElementArgs& a, const ElementLaunch& l, cudaStream_t stream);

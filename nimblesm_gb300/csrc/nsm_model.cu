@@ -87,7 +87,7 @@ struct nsm_model {
   int     closure_first = 0, num_exact = 0;
   nsm::GroupMaterial* d_mats = nullptr;  // [num_mats]
   std::vector<double> dt_group;    // per-sample critical time step
-  nsm::ElementLaunch  elaunch{128, 0, 0};
+  nsm::ElementLaunch  elaunch{128, 0, 0, 0};
   nsm_mlp*            closure = nullptr;        // learned material (FP32 form), or null
   unsigned long long* d_fallbacks = nullptr;    // points that left the closure's envelope
 
@@ -1047,45 +1047,71 @@ int nsm_time_kernels(nsm_model* m, int repeats, double* element_ms, double* node
   return read_status(m);
 }
 
-// Element-kernel launch shapes the autotuner tries: elements per block, and
-// one pass (one thread per element) or a persistent grid of blocks per SM
-// walking the elements of all samples.
+// Element-kernel launch shapes the autotuner tries: elements per block; one
+// pass (one thread per element; blocks_per_sm > 0 then bounds the registers
+// so that many 128-thread blocks fit an SM, FP64 form) or a persistent grid of
+// blocks per SM walking the elements of all samples; and, in the FP32 form,
+// the persistent grid with the nodal values staged one element ahead.
+// Shapes a form does not have fall back to its plain launch.
 static const nsm::ElementLaunch kLaunchCandidates[] = {
-    {128, 0, 0}, {64, 0, 0}, {128, 1, 1}, {128, 1, 2}, {128, 1, 4}, {64, 1, 2}, {64, 1, 4}, {64, 1, 8},
+    {128, 0, 0, 0}, {64, 0, 0, 0},  {128, 1, 1, 0}, {128, 1, 2, 0}, {128, 1, 4, 0}, {64, 1, 2, 0},
+    {64, 1, 4, 0},  {64, 1, 8, 0},  {128, 0, 3, 0}, {128, 1, 3, 1}, {64, 1, 6, 1},
 };
 static const int kNumLaunchCandidates = sizeof(kLaunchCandidates) / sizeof(kLaunchCandidates[0]);
+
+int nsm_launch_candidate_times(nsm_model* m, int repeats, double* ms, int capacity, int* count)
+{
+  if (!m || repeats <= 0 || (capacity > 0 && !ms)) return fail(NSM_ERR_INVALID_ARGUMENT, "invalid argument");
+  if (count) *count = kNumLaunchCandidates;
+  NSM_CUDA(cudaSetDevice(m->device));
+  const nsm::ElementLaunch keep = m->elaunch;
+  cudaEvent_t              a, b;
+  NSM_CUDA(cudaEventCreate(&a));
+  NSM_CUDA(cudaEventCreate(&b));
+  cudaError_t err = cudaSuccess;
+  for (int c = 0; c < kNumLaunchCandidates && c < capacity && err == cudaSuccess; c++) {
+    m->elaunch = kLaunchCandidates[c];
+    err        = launch_element(m, -1);  // warm
+    if (err == cudaSuccess) err = cudaEventRecord(a, m->stream);
+    for (int r = 0; r < repeats && err == cudaSuccess; r++) err = launch_element(m, -1);
+    if (err == cudaSuccess) err = cudaEventRecord(b, m->stream);
+    if (err == cudaSuccess) err = cudaEventSynchronize(b);
+    float t = 0;
+    if (err == cudaSuccess) err = cudaEventElapsedTime(&t, a, b);
+    ms[c] = t / repeats;
+  }
+  m->elaunch = keep;
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  NSM_CUDA(err);
+  return read_status(m);
+}
+
+int nsm_set_launch_candidate(nsm_model* m, int candidate)
+{
+  if (!m || candidate < 0 || candidate >= kNumLaunchCandidates)
+    return fail(NSM_ERR_INVALID_ARGUMENT, "invalid launch candidate");
+  m->elaunch = kLaunchCandidates[candidate];
+  for (auto& g : m->graphs) cudaGraphExecDestroy(g.second);  // captured with the old shape
+  m->graphs.clear();
+  return NSM_OK;
+}
 
 int nsm_autotune(nsm_model* m, int repeats, int* chosen, double* best_ms)
 {
   if (!m || repeats <= 0) return fail(NSM_ERR_INVALID_ARGUMENT, "invalid argument");
-  NSM_CUDA(cudaSetDevice(m->device));
-  cudaEvent_t a, b;
-  NSM_CUDA(cudaEventCreate(&a));
-  NSM_CUDA(cudaEventCreate(&b));
-  int    best = 0;
-  double best_t = 1e300;
-  for (int c = 0; c < kNumLaunchCandidates; c++) {
-    m->elaunch = kLaunchCandidates[c];
-    NSM_CUDA(launch_element(m, -1));  // warm
-    cudaEventRecord(a, m->stream);
-    for (int r = 0; r < repeats; r++) NSM_CUDA(launch_element(m, -1));
-    cudaEventRecord(b, m->stream);
-    NSM_CUDA(cudaEventSynchronize(b));
-    float ms = 0;
-    cudaEventElapsedTime(&ms, a, b);
-    if (ms < best_t) {
-      best_t = ms;
-      best   = c;
-    }
-  }
-  cudaEventDestroy(a);
-  cudaEventDestroy(b);
+  double t[kNumLaunchCandidates];
+  int    rc = nsm_launch_candidate_times(m, repeats, t, kNumLaunchCandidates, nullptr);
+  if (rc != NSM_OK) return rc;
+  int best = 0;
+  for (int c = 1; c < kNumLaunchCandidates; c++)
+    if (t[c] < t[best]) best = c;
   m->elaunch = kLaunchCandidates[best];
   for (auto& g : m->graphs) cudaGraphExecDestroy(g.second);  // captured with the old shape
   m->graphs.clear();
   if (chosen) *chosen = best;
-  if (best_ms) *best_ms = best_t / repeats;
-  return read_status(m);
+  if (best_ms) *best_ms = t[best];
+  return NSM_OK;
 }
 
 int nsm_set_mlp_closure(nsm_model* m, nsm_mlp* closure)

@@ -64,8 +64,10 @@ __device__ __forceinline__ double invert3x3(const double m[3][3], double inv[3][
 
 // Per element: the reference Jacobian J_X = sum_j X_j (x) dN_j/dxi at each
 // integration point, accumulated as src/nimble_element.h:458-491 does, its
-// inverse G0 = J_X^{-1} and determinant (stored as planes geo[ip*10 + q][E]:
-// q = 0..8 G0[k][J] row-major, q = 9 det J_X); the element's lumped mass
+// inverse, determinant and the determinant's reciprocal (planes
+// geo[ip * kGeoPerPoint + q][E], scaled for the modal gradient: q = 0..8
+// J_X^{-1} / 8, q = 9 det J_X, q = 10..18 8 J_X, q = 19 1 / (512 det J_X));
+// the element's lumped mass
 // (src/nimble_element.h:266-309, src/nimble_element.cc:173-193) as planes
 // me[c][E]; and the element's stable time step L_e / sqrt(K/rho)
 // (src/nimble_block_base.cc:51-84, src/nimble_element.cc:221-260).
@@ -102,13 +104,15 @@ __global__ void k_setup_elements(int E, long ld_e, const int* __restrict__ conn,
     double det = invert3x3(b, bi);
     jdet[ip]   = det;
     if (!(det > 0.0)) bad = true;
+    // scaled for the modal gradient (8 du/dxi), by powers of two (exact):
+    // J_X^{-1} / 8, 8 J_X and 1 / (512 det J_X); det J_X itself unscaled
     for (int k = 0; k < 3; k++)
       for (int J = 0; J < 3; J++) {
-        geo[(ip * kGeoPerPoint + k * 3 + J) * ld_e + e]      = bi[k][J];
-        geo[(ip * kGeoPerPoint + 10 + k * 3 + J) * ld_e + e] = b[k][J];
+        geo[(ip * kGeoPerPoint + k * 3 + J) * ld_e + e]      = bi[k][J] * 0.125;
+        geo[(ip * kGeoPerPoint + 10 + k * 3 + J) * ld_e + e] = b[k][J] * 8.0;
       }
     geo[(ip * kGeoPerPoint + 9) * ld_e + e]  = det;
-    geo[(ip * kGeoPerPoint + 19) * ld_e + e] = 1.0 / det;
+    geo[(ip * kGeoPerPoint + 19) * ld_e + e] = (1.0 / det) * (1.0 / 512.0);
   }
   for (int i = 0; i < 8; i++) {
     double m = 0.0;

@@ -97,6 +97,8 @@ SIGNATURES = {
     "nsm_ensemble_max_abs": (C.c_int, [_vp, C.c_int, C.c_int, _ip, C.c_int, _dp]),
     "nsm_begin_ensemble": (C.c_int, [_vp, C.c_double, _dp, C.c_int, C.c_int, _dp]),
     "nsm_autotune": (C.c_int, [_vp, C.c_int, _ip, _dp]),
+    "nsm_launch_candidate_times": (C.c_int, [_vp, C.c_int, _dp, C.c_int, _ip]),
+    "nsm_set_launch_candidate": (C.c_int, [_vp, C.c_int]),
     "nsm_critical_time_step_noalloc": (C.c_int, [C.c_int, C.c_int, _vp, _vp, _vp, C.c_double, C.c_double, _vp,
                                                 _vp]),
     "nsm_mlp_last_error": (C.c_char_p, []),
@@ -322,6 +324,17 @@ class Model:
         c, ms = C.c_int(), C.c_double()
         _check(library().nsm_autotune(self._h, repeats, C.byref(c), C.byref(ms)))
         return c.value, ms.value
+
+    def set_launch_candidate(self, candidate):
+        _check(library().nsm_set_launch_candidate(self._h, int(candidate)))
+
+    def launch_candidate_times(self, repeats=5):
+        """Mean element-kernel milliseconds of every candidate launch shape."""
+        n = C.c_int()
+        _check(library().nsm_launch_candidate_times(self._h, repeats, None, 0, C.byref(n)))
+        ms = (C.c_double * n.value)()
+        _check(library().nsm_launch_candidate_times(self._h, repeats, ms, n.value, None))
+        return list(ms)
 
     def advance(self, num_steps):
         _check(library().nsm_advance(self._h, int(num_steps)))

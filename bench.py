@@ -40,11 +40,14 @@ METRIC = "hex8 IP stress updates/sec, plain FP64 vs mixed/MLP at <=1e-3 rel. dis
 UNIT = "IP-updates/s"
 SCHEDULE_STEPS = 2000  # the workload's schedule: dt = 0.5 dt_crit, 2000 steps
 # FP64 work per integration point of the FP64 element kernel's formulation:
-# 95.4 DFMA (2 flops each) + 31.8 DADD + 54.7 DMUL executed per point (ncu on
+# 87.9 DFMA (2 flops each) + 47.5 DADD + 37.9 DMUL executed per point (ncu on
 # the 64^3 case, profiles/k_element_fp64_cube64.md).  The FP64 pipe issues
 # 2 of these instructions per SM per cycle, whatever their kind.
-FP64_FLOPS_PER_IP = 277.2
-FP64_INSTR_PER_IP = 181.9
+FP64_FLOPS_PER_IP = 261.1
+FP64_INSTR_PER_IP = 173.2
+# DRAM bytes (read + write) of one element launch on the 128^3 cube, from one
+# ncu capture per form (profiles/k_element_traffic_cube128.md).
+ELEMENT_TRAFFIC_128 = {"fp64": 2.671848192e9 + 2.499607296e9, "fp32": 0.119998720e9 + 1.217577728e9}
 
 
 def algorithmic_bytes(N, E, precision):
@@ -412,7 +415,10 @@ def run_ours(args):
                 "path": "nsm_compute_internal_force_host (pinned u in, f_int out)", "steps": e2e_steps},
         "gpu_launches": head["launches"],
         "roofline": {"bound": "hbm", "kernel": "k_element", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
+                     "frac": achieved / peak, "peak_source": peak_kind,
+                     "traffic": ELEMENT_TRAFFIC_128.get(args.precision) if n == 128 else None,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, one 128^3 launch"
+                     if n == 128 else None,
                      "algorithmic_bytes_per_launch": elem_bytes, "launch_ms": elem_ms, "node_launch_ms": node_ms,
                      "step_algorithmic_bytes": step_bytes},
         "clocks": head["clocks"],

@@ -412,7 +412,8 @@ def run_ours(args):
                    "dt": dt, "schedule_steps": sched, "parallelism": f"replicas{ws}",
                    "l2": "inputs larger than L2 (per-step traffic >> 129 MB)"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 24 * N, "d2h_bytes_per_step": 24 * N,
-                "path": "nsm_compute_internal_force_host (pinned u in, f_int out)", "steps": e2e_steps},
+                "path": "nsm_compute_internal_force_host (pinned u in, f_int out)", "steps": e2e_steps,
+                "host_chunks": m.host_chunks()},
         "gpu_launches": head["launches"],
         "roofline": {"bound": "hbm", "kernel": "k_element", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind,

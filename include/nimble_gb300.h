@@ -189,6 +189,14 @@ int nsm_compute_internal_force(nsm_model* model, double time_previous, double ti
  * reference's integrator loop (which updates nodes on the host) calls each
  * step through a GpuModelData.  displacement, internal_force: [N][3]. */
 int nsm_compute_internal_force_host(nsm_model* model, const double* displacement, double* internal_force);
+/* The host-buffer call runs as a pipeline of `chunks` element ranges: u is
+ * copied in by node ranges ahead of the element launches that need them and
+ * f_int copied out by node ranges as soon as their elements are done, so the
+ * copies overlap the element kernel (pinned buffers).  The result is bitwise
+ * that of one launch.  0 restores the default (8 for 262,144 elements or
+ * more, else 1); the learned and UQ closures always run as one chunk. */
+int nsm_set_host_chunks(nsm_model* model, int chunks);
+int nsm_host_chunks(nsm_model* model, int* chunks);
 
 /* Element data of the last internal-force evaluation, reference layout
  * (ModelData element data n/np1, src/nimble_model_data.cc:142-169).

@@ -73,10 +73,11 @@ template <typename T, bool kPrecomputedGeo, bool kPersistent, int kMinBlocks = 1
 __global__ void __launch_bounds__(128, kMinBlocks) k_element(ElementArgs a)
 {
   if constexpr (!kPersistent) {
-    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    const int e = a.e_begin + blockIdx.x * blockDim.x + threadIdx.x;
     if (e < a.E) element_work<T, kPrecomputedGeo>(a, e, GlobalNodes<T>(a, e));
   } else {
-    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < a.E; e += (long)gridDim.x * blockDim.x)
+    for (long e = a.e_begin + blockIdx.x * (long)blockDim.x + threadIdx.x; e < a.E;
+         e += (long)gridDim.x * blockDim.x)
       element_work<T, kPrecomputedGeo>(a, (int)e, GlobalNodes<T>(a, (int)e));
   }
 }
@@ -128,7 +129,7 @@ __global__ void __launch_bounds__(128, 3) k_element_staged(ElementArgs a)
   const int  slot   = kStageWords * B;
   float*     cur    = stage_mem + threadIdx.x;  // slot of the element being computed
   float*     nxt    = cur + slot;               // slot of the next one
-  long       e      = blockIdx.x * (long)B + threadIdx.x;
+  long       e      = a.e_begin + blockIdx.x * (long)B + threadIdx.x;
   // prologue: connectivity of e (waited for), its nodal values and the
   // connectivity of e + stride in flight
   if (e < a.E) stage_conn(a, e, reinterpret_cast<int*>(cur + kStageValues * B), B);
@@ -317,10 +318,10 @@ int num_sms()
 template <typename T, bool kGeo>
 static cudaError_t launch_element(ElementArgs a, const ElementLaunch& l, cudaStream_t stream)
 {
-  if (a.E == 0) return cudaSuccess;
+  if (a.E <= a.e_begin) return cudaSuccess;
   const int block = (l.block == 64 || l.block == 128) ? l.block : 128;
   a.persistent    = l.persistent;
-  int grid        = grid_for(a.E, block);
+  int grid        = grid_for(a.E - a.e_begin, block);
   if (l.persistent) {
     int g = l.blocks_per_sm * num_sms();
     if (g < grid) grid = g;
@@ -345,7 +346,7 @@ cudaError_t launch_element_fp64(const ElementArgs& a, const ElementLaunch& l, cu
 cudaError_t launch_element_fp32(const ElementArgs& a, const ElementLaunch& l, cudaStream_t stream)
 {
   if (!l.staged) return launch_element<float, false>(a, l, stream);
-  if (a.E == 0) return cudaSuccess;
+  if (a.E <= a.e_begin) return cudaSuccess;
   const int    block = (l.block == 64 || l.block == 128) ? l.block : 128;
   const size_t smem  = 2 * kStageWords * block * sizeof(float);
   static bool  configured = false;
@@ -360,7 +361,7 @@ cudaError_t launch_element_fp32(const ElementArgs& a, const ElementLaunch& l, cu
   }
   ElementArgs  b     = a;
   b.persistent       = 1;
-  int grid           = grid_for(a.E, block);
+  int grid           = grid_for(a.E - a.e_begin, block);
   const int g        = (l.blocks_per_sm > 0 ? l.blocks_per_sm : 1) * num_sms();
   if (g < grid) grid = g;
   k_element_staged<<<grid, block, smem, stream>>>(b);
@@ -527,11 +528,14 @@ __global__ void k_node_soa_to_aos(int N, long ld_n, const double* __restrict__ s
   dst[i] = src[(i % 3) * ld_n + i / 3];
 }
 
-__global__ void k_node_aos_to_soa(int N, long ld_n, const double* __restrict__ src, double* __restrict__ dst)
+__global__ void k_node_aos_to_soa(int N, long ld_n, const double* __restrict__ src, double* __restrict__ dst,
+                                  float* __restrict__ dstf)
 {
   long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= 3L * N) return;
-  dst[(i % 3) * ld_n + i / 3] = src[i];
+  const double x = src[i];
+  dst[(i % 3) * ld_n + i / 3] = x;
+  if (dstf) dstf[(i % 3) * ld_n + i / 3] = (float)x;
 }
 
 cudaError_t launch_node_soa_to_aos(int N, long ld_n, const double* src, double* dst, cudaStream_t stream)
@@ -541,10 +545,11 @@ cudaError_t launch_node_soa_to_aos(int N, long ld_n, const double* src, double* 
   return cudaGetLastError();
 }
 
-cudaError_t launch_node_aos_to_soa(int N, long ld_n, const double* src, double* dst, cudaStream_t stream)
+cudaError_t launch_node_aos_to_soa(int N, long ld_n, const double* src, double* dst, float* dstf,
+                                   cudaStream_t stream)
 {
   if (N == 0) return cudaSuccess;
-  k_node_aos_to_soa<<<grid_for(3L * N, 256), 256, 0, stream>>>(N, ld_n, src, dst);
+  k_node_aos_to_soa<<<grid_for(3L * N, 256), 256, 0, stream>>>(N, ld_n, src, dst, dstf);
   return cudaGetLastError();
 }
 

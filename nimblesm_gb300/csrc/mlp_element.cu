@@ -430,6 +430,7 @@ cudaError_t setup_element_kernel()
 cudaError_t launch_element_mlp(const ElementArgs& a, const MlpElementArgs& m, cudaStream_t stream)
 {
   if (a.E == 0) return cudaSuccess;
+  if (a.e_begin != 0) return cudaErrorInvalidValue;  // the closure kernel runs over all elements
   const long chunks = (a.E + el::kElems - 1) / el::kElems;
   const long cap    = (long)num_sms() * (g_blocks_per_sm > 0 ? g_blocks_per_sm : 1);
   const int  grid   = (int)(chunks < cap ? chunks : cap);

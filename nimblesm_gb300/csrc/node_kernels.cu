@@ -58,7 +58,7 @@ __device__ __forceinline__ void gather_force(const NodeArgs& a, int n, double f[
 template <typename TF, bool kExact>
 __global__ void __launch_bounds__(256) k_node_update(NodeArgs a)
 {
-  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n = a.n_begin + blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= a.N) return;
   const long ld = a.ld_n;
   double     u[3], v[3], acc[3];
@@ -133,11 +133,11 @@ __global__ void __launch_bounds__(256) k_node_update(NodeArgs a)
 
 cudaError_t launch_node_update(const NodeArgs& a, cudaStream_t stream)
 {
-  if (a.N == 0) return cudaSuccess;
+  if (a.N <= a.n_begin) return cudaSuccess;
   if (a.fe_is_float)
-    k_node_update<float, false><<<grid_for(a.N, 256), 256, 0, stream>>>(a);
+    k_node_update<float, false><<<grid_for(a.N - a.n_begin, 256), 256, 0, stream>>>(a);
   else
-    k_node_update<double, true><<<grid_for(a.N, 256), 256, 0, stream>>>(a);
+    k_node_update<double, true><<<grid_for(a.N - a.n_begin, 256), 256, 0, stream>>>(a);
   return cudaGetLastError();
 }
 

@@ -66,7 +66,8 @@ constexpr int kIpRecord = 16;
 
 // Element kernel arguments (one launch = all elements of a block).
 struct ElementArgs {
-  int           E;
+  int           E;         // elements [e_begin, E) are computed by this launch
+  int           e_begin;
   long          ld_e, ld_n;
   const int*    conn;      // [8][ld_e]
   const double* u;         // [3][ld_n] displacement (FP64 form)
@@ -104,7 +105,8 @@ cudaError_t launch_ip_identity(int E, long ld_e, void* ip, int ip_is_float, cuda
 // Node kernel: the end of step s (gather f_int, a = f/m, v += half*a, output
 // BCs) fused with the start of step s+1 (v += half*a, BCs, u += delta*v, BCs).
 struct NodeArgs {
-  int               N;
+  int               N;        // nodes [n_begin, N) are updated by this launch
+  int               n_begin;
   long              ld_n, ld_e;
   const int*        node_ptr;
   const int*        node_inc;
@@ -159,6 +161,8 @@ cudaError_t launch_ip_to_aos(int E, long ld_e, const void* ip, int src_is_float,
                              cudaStream_t stream);
 cudaError_t launch_to_float(long n, const double* src, float* dst, cudaStream_t stream);
 cudaError_t launch_node_soa_to_aos(int N, long ld_n, const double* src, double* dst, cudaStream_t stream);
-cudaError_t launch_node_aos_to_soa(int N, long ld_n, const double* src, double* dst, cudaStream_t stream);
+// dstf (nullable): also an FP32 copy of the planes, same layout.
+cudaError_t launch_node_aos_to_soa(int N, long ld_n, const double* src, double* dst, float* dstf,
+                                   cudaStream_t stream);
 
 }  // namespace nsm

@@ -5,6 +5,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <algorithm>
 #include <map>
 #include <string>
 #include <vector>
@@ -108,6 +109,18 @@ struct nsm_model {
 
   std::map<int, cudaGraphExec_t> graphs;
 
+  // Host-buffer pipeline (nsm_compute_internal_force_host): K element chunks,
+  // the copy of u in by node ranges ahead of them and the copy of f_int out
+  // by node ranges behind them.  hp_e[j]..hp_e[j+1] are chunk j's elements;
+  // nodes [0, hp_in[j+1]) cover every node of chunks 0..j; every element of
+  // nodes [0, hp_ready[j+1]) is in chunks 0..j.
+  int                      host_chunks = -1;  // requested (-1: by size)
+  int                      hp_k = 0;          // chunks the cut tables were built for
+  std::vector<int>         hp_e, hp_in, hp_ready;
+  cudaStream_t             hp_stream[4] = {};  // copy in, elements (2), copy out
+  std::vector<cudaEvent_t> hp_ev;              // [0]: start; then per chunk: in, elements, gathered
+  double*                  d_stage_out = nullptr;
+
   // profiling
   bool                                              profiling = false;
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_elem, ev_node;
@@ -126,9 +139,14 @@ void free_all(nsm_model* m)
                   m->d_f,    m->d_fext,     m->d_mass,     m->d_inv_mass, m->d_geo,    m->d_ip,    m->d_Xf,
                   m->d_uf,   m->d_fe,   m->d_status,   m->d_step_base, m->d_scratch, m->d_stage,  m->d_out,   m->d_bc_slot,
                   m->d_bcs,  m->d_ibc_slot, m->d_ibcs,     m->d_sched, m->d_group_out, m->d_elem_group,
-                  m->d_node_group, m->d_elem_off, m->d_mats, m->d_fallbacks, m->d_node_off, m->d_closure};
+                  m->d_node_group, m->d_elem_off, m->d_mats, m->d_fallbacks, m->d_node_off, m->d_closure,
+                  m->d_stage_out};
   for (void* p : ptrs)
     if (p) cudaFree(p);
+  for (cudaStream_t s : m->hp_stream)
+    if (s) cudaStreamDestroy(s);
+  for (cudaEvent_t e : m->hp_ev) cudaEventDestroy(e);
+  m->hp_ev.clear();
   for (auto& e : m->ev_elem) {
     cudaEventDestroy(e.first);
     cudaEventDestroy(e.second);
@@ -213,6 +231,7 @@ nsm::ElementArgs element_args(nsm_model* m, int k)
 {
   nsm::ElementArgs a;
   a.E         = m->E;
+  a.e_begin   = 0;
   a.ld_e      = m->ld_e;
   a.ld_n      = m->ld_n;
   a.conn      = m->d_conn;
@@ -241,6 +260,7 @@ nsm::NodeArgs node_args(nsm_model* m, int k_post, int k_pre, int gather_only)
 {
   nsm::NodeArgs a;
   a.N           = m->N;
+  a.n_begin     = 0;
   a.ld_n        = m->ld_n;
   a.ld_e        = m->ld_e;
   a.node_ptr    = m->d_node_ptr;
@@ -782,7 +802,7 @@ int nsm_set_node_field(nsm_model* m, int field, const double* values)
   NSM_CUDA(cudaSetDevice(m->device));
   if (m->N == 0) return NSM_OK;
   NSM_CUDA(cudaMemcpyAsync(m->d_stage, values, sizeof(double) * 3 * m->N, cudaMemcpyHostToDevice, m->stream));
-  NSM_CUDA(nsm::launch_node_aos_to_soa(m->N, m->ld_n, m->d_stage, dst, m->stream));
+  NSM_CUDA(nsm::launch_node_aos_to_soa(m->N, m->ld_n, m->d_stage, dst, nullptr, m->stream));
   if (dst == m->d_u) NSM_CUDA(sync_uf(m));
   NSM_CUDA(cudaStreamSynchronize(m->stream));
   return NSM_OK;
@@ -810,15 +830,149 @@ int nsm_compute_internal_force(nsm_model* m, double, double, int)
   return read_status(m);
 }
 
+namespace {
+
+// Chunks of the host-buffer pipeline: none for the closures (the learned
+// closure's kernel runs over all elements; a UQ sample's nodes gather the
+// forces of other samples' elements) or a small mesh.
+int host_chunk_count(const nsm_model* m)
+{
+  if (m->closure || m->d_closure) return 1;
+  int k = m->host_chunks > 0 ? m->host_chunks : (m->E >= (1 << 18) ? 8 : 1);
+  if (k > m->E) k = m->E > 0 ? m->E : 1;
+  return k;
+}
+
+// Cut tables for K chunks from the connectivity (copied back once per K).
+cudaError_t build_host_pipe(nsm_model* m, int K)
+{
+  const int        E = m->E, N = m->N;
+  std::vector<int> conn((size_t)8 * m->ld_e);
+  cudaError_t      err = cudaMemcpy(conn.data(), m->d_conn, sizeof(int) * conn.size(), cudaMemcpyDeviceToHost);
+  if (err != cudaSuccess) return err;
+  std::vector<int> elem_hi(E);      // largest node of elements 0..e
+  std::vector<int> node_last(N, -1);  // largest element of node n, then of nodes 0..n
+  int              hi = -1;
+  for (int e = 0; e < E; e++) {
+    for (int c = 0; c < 8; c++) {
+      const int id = conn[(size_t)c * m->ld_e + e];
+      hi           = id > hi ? id : hi;
+      if (e > node_last[id]) node_last[id] = e;
+    }
+    elem_hi[e] = hi;
+  }
+  for (int n = 1; n < N; n++) node_last[n] = node_last[n] > node_last[n - 1] ? node_last[n] : node_last[n - 1];
+  m->hp_e.assign(K + 1, 0);
+  m->hp_in.assign(K + 1, 0);
+  m->hp_ready.assign(K + 1, 0);
+  for (int j = 1; j <= K; j++) {
+    m->hp_e[j]     = (int)((long)E * j / K);
+    const int need = m->hp_e[j] > 0 ? elem_hi[m->hp_e[j] - 1] + 1 : 0;
+    m->hp_in[j]    = j == K ? N : (need > m->hp_in[j - 1] ? need : m->hp_in[j - 1]);
+    // first node with an element at or after the chunk's end
+    const int* r   = std::lower_bound(node_last.data(), node_last.data() + N, m->hp_e[j]);
+    m->hp_ready[j] = j == K ? N : (int)(r - node_last.data());
+  }
+  if ((int)m->hp_ev.size() < 1 + 3 * K) {
+    for (cudaEvent_t e : m->hp_ev) cudaEventDestroy(e);
+    m->hp_ev.assign(1 + 3 * K, nullptr);
+    for (auto& e : m->hp_ev)
+      if ((err = cudaEventCreateWithFlags(&e, cudaEventDisableTiming)) != cudaSuccess) return err;
+  }
+  for (auto& s : m->hp_stream)
+    if (!s && (err = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking)) != cudaSuccess) return err;
+  if (!m->d_stage_out && (err = cudaMalloc(&m->d_stage_out, sizeof(double) * 3 * (size_t)N)) != cudaSuccess)
+    return err;
+  m->hp_k = K;
+  return cudaSuccess;
+}
+
+// The pipelined host-buffer evaluation: every element's arithmetic and every
+// node's gather order are those of the one-launch path, so the result is
+// bitwise the same.
+cudaError_t internal_force_pipelined(nsm_model* m, const double* u_host, double* f_host, int K)
+{
+  cudaStream_t s_in = m->hp_stream[0], s_out = m->hp_stream[3];
+  cudaStream_t s_el[2] = {m->hp_stream[1], m->hp_stream[2]};
+  cudaEvent_t* ev      = m->hp_ev.data();  // ev[0] start; ev[1 + 3j + {0, 1, 2}] in, elements, gathered
+  cudaError_t  err     = cudaEventRecord(ev[0], m->stream);  // earlier work on the state is done first
+  if (err == cudaSuccess) err = cudaStreamWaitEvent(s_in, ev[0], 0);
+  for (int j = 0; j < K && err == cudaSuccess; j++) {
+    const int n0 = m->hp_in[j], n1 = m->hp_in[j + 1];
+    if (n1 > n0) {
+      err = cudaMemcpyAsync(m->d_stage + 3L * n0, u_host + 3L * n0, sizeof(double) * 3 * (size_t)(n1 - n0),
+                            cudaMemcpyHostToDevice, s_in);
+      if (err == cudaSuccess)
+        err = nsm::launch_node_aos_to_soa(n1 - n0, m->ld_n, m->d_stage + 3L * n0, m->d_u + n0,
+                                          m->d_uf ? m->d_uf + n0 : nullptr, s_in);
+    }
+    if (err == cudaSuccess) err = cudaEventRecord(ev[1 + 3 * j], s_in);
+  }
+  for (int j = 0; j < K && err == cudaSuccess; j++) {
+    cudaStream_t s = s_el[j & 1];
+    err            = cudaStreamWaitEvent(s, ev[1 + 3 * j], 0);
+    if (err == cudaSuccess) {
+      nsm::ElementArgs a = element_args(m, -1);
+      a.e_begin          = m->hp_e[j];
+      a.E                = m->hp_e[j + 1];
+      err = m->precision == NSM_PRECISION_FP64 ? nsm::launch_element_fp64(a, m->elaunch, s)
+                                               : nsm::launch_element_fp32(a, m->elaunch, s);
+    }
+    if (err == cudaSuccess) err = cudaEventRecord(ev[2 + 3 * j], s);
+  }
+  for (int j = 0; j < K && err == cudaSuccess; j++) {
+    // chunks 0..j done: the last one on each element stream
+    err = cudaStreamWaitEvent(m->stream, ev[2 + 3 * j], 0);
+    if (err == cudaSuccess && j > 0) err = cudaStreamWaitEvent(m->stream, ev[2 + 3 * (j - 1)], 0);
+    const int r0 = m->hp_ready[j], r1 = m->hp_ready[j + 1];
+    if (err == cudaSuccess && r1 > r0) {
+      nsm::NodeArgs a = node_args(m, -1, -1, 1);
+      a.n_begin       = r0;
+      a.N             = r1;
+      err             = nsm::launch_node_update(a, m->stream);
+      if (err == cudaSuccess)
+        err = nsm::launch_node_soa_to_aos(r1 - r0, m->ld_n, m->d_f + r0, m->d_stage_out + 3L * r0, m->stream);
+    }
+    if (err == cudaSuccess) err = cudaEventRecord(ev[3 + 3 * j], m->stream);
+    if (err == cudaSuccess) err = cudaStreamWaitEvent(s_out, ev[3 + 3 * j], 0);
+    if (err == cudaSuccess && r1 > r0)
+      err = cudaMemcpyAsync(f_host + 3L * r0, m->d_stage_out + 3L * r0, sizeof(double) * 3 * (size_t)(r1 - r0),
+                            cudaMemcpyDeviceToHost, s_out);
+  }
+  if (err == cudaSuccess) err = cudaStreamSynchronize(s_out);
+  return err;
+}
+
+}  // namespace
+
+int nsm_set_host_chunks(nsm_model* m, int chunks)
+{
+  if (!m || chunks < 0 || chunks > 256) return fail(NSM_ERR_INVALID_ARGUMENT, "invalid chunk count");
+  m->host_chunks = chunks == 0 ? -1 : chunks;
+  return NSM_OK;
+}
+
+int nsm_host_chunks(nsm_model* m, int* chunks)
+{
+  if (!m || !chunks) return fail(NSM_ERR_INVALID_ARGUMENT, "null argument");
+  *chunks = host_chunk_count(m);
+  return NSM_OK;
+}
+
 int nsm_compute_internal_force_host(nsm_model* m, const double* displacement, double* internal_force)
 {
   if (!m || !displacement || !internal_force) return fail(NSM_ERR_INVALID_ARGUMENT, "null argument");
   NSM_CUDA(cudaSetDevice(m->device));
   if (m->N == 0) return NSM_OK;
+  const int K = host_chunk_count(m);
+  if (K > 1) {
+    if (m->hp_k != K) NSM_CUDA(build_host_pipe(m, K));
+    NSM_CUDA(internal_force_pipelined(m, displacement, internal_force, K));
+    return read_status(m);  // synchronizes
+  }
   const size_t bytes = sizeof(double) * 3 * m->N;
   NSM_CUDA(cudaMemcpyAsync(m->d_stage, displacement, bytes, cudaMemcpyHostToDevice, m->stream));
-  NSM_CUDA(nsm::launch_node_aos_to_soa(m->N, m->ld_n, m->d_stage, m->d_u, m->stream));
-  NSM_CUDA(sync_uf(m));
+  NSM_CUDA(nsm::launch_node_aos_to_soa(m->N, m->ld_n, m->d_stage, m->d_u, m->d_uf, m->stream));
   NSM_CUDA(launch_element(m, -1));
   NSM_CUDA(nsm::launch_node_update(node_args(m, -1, -1, 1), m->stream));
   NSM_CUDA(nsm::launch_node_soa_to_aos(m->N, m->ld_n, m->d_f, m->d_stage, m->stream));

@@ -77,6 +77,8 @@ SIGNATURES = {
     "nsm_get_node_field": (C.c_int, [_vp, C.c_int, _dp]),
     "nsm_compute_internal_force": (C.c_int, [_vp, C.c_double, C.c_double, C.c_int]),
     "nsm_compute_internal_force_host": (C.c_int, [_vp, _dp, _dp]),
+    "nsm_set_host_chunks": (C.c_int, [_vp, C.c_int]),
+    "nsm_host_chunks": (C.c_int, [_vp, _ip]),
     "nsm_get_ip_data": (C.c_int, [_vp, _dp, _dp]),
     "nsm_compute_derived_element_data": (C.c_int, [_vp, _dp, _dp, _dp]),
     "nsm_get_energies": (C.c_int, [_vp, _dp, _dp]),
@@ -254,6 +256,15 @@ class Model:
 
     def ComputeInternalForce(self, time_previous=0.0, time_current=0.0, is_output_step=False):
         _check(library().nsm_compute_internal_force(self._h, time_previous, time_current, int(is_output_step)))
+
+    def set_host_chunks(self, chunks):
+        """Element ranges of the host-buffer pipeline (0: default)."""
+        _check(library().nsm_set_host_chunks(self._h, int(chunks)))
+
+    def host_chunks(self):
+        c = C.c_int()
+        _check(library().nsm_host_chunks(self._h, C.byref(c)))
+        return c.value
 
     def ComputeInternalForceHost(self, displacement, out=None) -> np.ndarray:
         u = np.ascontiguousarray(displacement, dtype=np.float64)

@@ -233,6 +233,40 @@ def test_host_buffer_internal_force_matches_device_path():
     assert rel(f_host, fo) < 1e-10
 
 
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_host_pipeline_chunks_give_the_same_bits(precision):
+    """The host-buffer call as a pipeline of element ranges (u copied in
+    ahead of them, f_int copied out behind them) equals the one-launch device
+    path bit for bit, at any chunk count: on a mesh in its natural order, on
+    one whose elements are shuffled (few nodes are complete before the last
+    chunk) and on an ensemble."""
+    rng = np.random.default_rng(5)
+    p = cube_problem(12, jitter=0.2, seed=31)
+    shuffled = cube_problem(10, jitter=0.2, seed=32)
+    shuffled.conn = np.ascontiguousarray(shuffled.conn[rng.permutation(shuffled.num_elem)])
+    ens = [cube_problem(n, jitter=0.2, seed=40 + n) for n in (6, 9, 4)]
+    for probs in ([p], [shuffled], ens):
+        m = E.Model(probs if len(probs) > 1 else probs[0], precision=precision)
+        N = m.problem.num_nodes
+        u = rng.normal(0, 1e-4, size=(N, 3))
+        m.SetVectorNodeData("displacement", u)
+        m.ComputeInternalForce()
+        ref = m.GetVectorNodeData("internal_force")
+        ref_F, ref_s = m.GetIntegrationPointData()
+        pin_u, pin_f = E.PinnedArray((N, 3)), E.PinnedArray((N, 3))
+        pin_u.array[:] = u
+        for k in (1, 2, 3, 7, 16):
+            m.set_host_chunks(k)
+            assert m.host_chunks() == k
+            pin_f.array[:] = np.nan
+            m.ComputeInternalForceHost(pin_u.array, pin_f.array)
+            assert np.array_equal(pin_f.array, ref), (len(probs), k)
+            F, sig = m.GetIntegrationPointData()
+            assert np.array_equal(F, ref_F) and np.array_equal(sig, ref_s), (len(probs), k)
+        m.set_host_chunks(0)
+        m.close()
+
+
 def test_fp32_mixed_within_1e3_of_fp64():
     p = cube_problem(16, jitter=0.2, seed=2)
     dt = 0.5 * critical_time_step(p)

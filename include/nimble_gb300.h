@@ -161,6 +161,22 @@ int nsm_ensemble_max_abs(nsm_model* model, int field, int component, const int* 
  * src/nimble_boundary_condition_manager.cc:52-72).  component 0..2. */
 int nsm_add_boundary_condition(nsm_model* model, int kind, int component, double value, const int* nodes,
                                int num_nodes);
+/* The same with the magnitude given by an expression f(x, y, z, t) (the
+ * quoted form of a deck line, BoundaryCondition::Initialize,
+ * src/nimble_boundary_condition.cc:102-117), evaluated at each node's
+ * reference coordinates and at time_current whenever the condition is applied
+ * (src/nimble_boundary_condition_manager.h:93-217).  The grammar is the
+ * reference's ExpressionParsing (src/nimble_expression_parser.h:522-695):
+ * + - * / % ^, unary -, ternary "c ? a : b" with | ^ & ! > >= < <= ==,
+ * sin cos tan erf exp log abs asin acos atan sqrt cbrt erfc ceil round floor
+ * log10, constants e pi tau.  NSM_ERR_INVALID_ARGUMENT with the parse error
+ * when the text does not parse. */
+int nsm_add_boundary_condition_expression(nsm_model* model, int kind, int component, const char* expression,
+                                          const int* nodes, int num_nodes);
+/* One host evaluation of an expression as the engine compiles it (the parse
+ * and the operation order of the device evaluation, with the host's math
+ * library), e.g. to check a deck's expressions before a run. */
+int nsm_bc_expression_eval(const char* expression, double x, double y, double z, double t, double* value);
 
 /* ModelData::ComputeLumpedMass (src/nimble_model_data.cc:495-530): the mass is
  * computed at nsm_create; this copies it out ([N], nullable). */

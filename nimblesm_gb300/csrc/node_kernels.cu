@@ -12,17 +12,97 @@
 
 namespace nsm {
 
-// ApplyKinematicBC for the explicit scheme, constant magnitudes
+// Value of expression program `prog` at node n and time t: the postfix
+// program on an operand stack, one double-precision operation at a time (no
+// contraction across operations).  The host refuses programs deeper than the
+// stack; a malformed one gives NaN rather than an access outside it.
+__device__ __noinline__ double eval_bc_expression(const BcExprTable& ex, int prog, int n, double t)
+{
+  const double x = ex.X[n], y = ex.X[ex.ld_n + n], z = ex.X[2 * ex.ld_n + n];
+  double       st[kExprStack];
+  int          sp = 0;
+  for (int i = ex.start[prog]; i < ex.start[prog + 1]; i++) {
+    const ExprOp o = ex.code[i];
+    if (o.code <= kExT) {
+      if (sp >= kExprStack) return NAN;
+      st[sp++] = o.code == kExConst ? o.c : (o.code == kExX ? x : (o.code == kExY ? y : (o.code == kExZ ? z : t)));
+      continue;
+    }
+    if (o.code == kExSelect) {
+      if (sp < 3) return NAN;
+      sp -= 2;
+      st[sp - 1] = st[sp - 1] != 0.0 ? st[sp] : st[sp + 1];
+      continue;
+    }
+    if (expr_is_unary(o.code)) {
+      if (sp < 1) return NAN;
+      const double a = st[sp - 1];
+      double       r;
+      switch (o.code) {
+        case kExNeg: r = -a; break;
+        case kExSin: r = sin(a); break;
+        case kExCos: r = cos(a); break;
+        case kExTan: r = tan(a); break;
+        case kExErf: r = erf(a); break;
+        case kExExp: r = exp(a); break;
+        case kExLog: r = log(a); break;
+        case kExAbs: r = fabs(a); break;
+        case kExAsin: r = asin(a); break;
+        case kExAcos: r = acos(a); break;
+        case kExAtan: r = atan(a); break;
+        case kExSqrt: r = sqrt(a); break;
+        case kExCbrt: r = cbrt(a); break;
+        case kExErfc: r = erfc(a); break;
+        case kExCeil: r = ceil(a); break;
+        case kExRound: r = round(a); break;
+        case kExFloor: r = floor(a); break;
+        case kExLog10: r = log10(a); break;
+        default: r = a != 0.0 ? 0.0 : 1.0; break;  // kExNot
+      }
+      st[sp - 1] = r;
+      continue;
+    }
+    if (sp < 2) return NAN;
+    const double a = st[sp - 2], b = st[sp - 1];
+    double       r;
+    switch (o.code) {
+      case kExAdd: r = __dadd_rn(a, b); break;
+      case kExSub: r = __dsub_rn(a, b); break;
+      case kExMul: r = __dmul_rn(a, b); break;
+      case kExDiv: r = __ddiv_rn(a, b); break;
+      case kExMod: r = fmod(a, b); break;
+      case kExPow: r = pow(a, b); break;
+      case kExGt: r = a > b ? 1.0 : 0.0; break;
+      case kExGe: r = a >= b ? 1.0 : 0.0; break;
+      case kExLt: r = a < b ? 1.0 : 0.0; break;
+      case kExLe: r = a <= b ? 1.0 : 0.0; break;
+      case kExEq: r = a == b ? 1.0 : 0.0; break;
+      case kExAnd: r = (a != 0.0 && b != 0.0) ? 1.0 : 0.0; break;
+      case kExOr: r = (a != 0.0 || b != 0.0) ? 1.0 : 0.0; break;
+      case kExXor: r = ((a != 0.0) != (b != 0.0)) ? 1.0 : 0.0; break;
+      default: return NAN;
+    }
+    st[--sp - 1] = r;
+  }
+  return sp == 1 ? st[0] : NAN;
+}
+
+// ApplyKinematicBC for the explicit scheme
 // (src/nimble_boundary_condition_manager.h:136-217): prescribed velocity sets
-// v; prescribed displacement sets v = (d - u) / delta when delta > 0.
-__device__ __forceinline__ void apply_bc(const NodeBC& bc, double delta, const double u[3], double v[3])
+// v; prescribed displacement sets v = (d - u) / delta when delta > 0.  The
+// magnitude is the line's constant or its expression at the node's reference
+// coordinates and time_current.
+__device__ __forceinline__ void apply_bc(const NodeBC& bc, double delta, double time, const BcExprTable& ex, int n,
+                                         const double u[3], double v[3])
 {
 #pragma unroll
   for (int k = 0; k < 3; k++) {
+    if (bc.kind[k] == 0 || (bc.kind[k] == 2 && !(delta > 0.0))) continue;
+    const double value = bc.expr[k] < 0 ? bc.value[k] : eval_bc_expression(ex, bc.expr[k], n, time);
     if (bc.kind[k] == 1) {
-      v[k] = bc.value[k];
-    } else if (bc.kind[k] == 2 && delta > 0.0) {
-      v[k] = __ddiv_rn(__dadd_rn(bc.value[k], -u[k]), delta);
+      v[k] = value;
+    } else {
+      v[k] = __ddiv_rn(__dadd_rn(value, -u[k]), delta);
     }
   }
 }
@@ -102,7 +182,7 @@ __global__ void __launch_bounds__(256) k_node_update(NodeArgs a)
       v[i]   = axpy<kExact>(s.half, acc[i], a.v[i * ld + n]);
       u[i]   = a.u[i * ld + n];
     }
-    if (s.is_output && slot >= 0) apply_bc(bc, s.delta, u, v);
+    if (s.is_output && slot >= 0) apply_bc(bc, s.delta, s.time, a.ex, n, u, v);
   } else {
 #pragma unroll
     for (int i = 0; i < 3; i++) {
@@ -117,10 +197,10 @@ __global__ void __launch_bounds__(256) k_node_update(NodeArgs a)
     const StepSched s = a.sched[(long)(*a.step_base + a.k_pre) * a.num_groups + group];
 #pragma unroll
     for (int i = 0; i < 3; i++) v[i] = axpy<kExact>(s.half, acc[i], v[i]);
-    if (slot >= 0) apply_bc(bc, s.delta, u, v);
+    if (slot >= 0) apply_bc(bc, s.delta, s.time, a.ex, n, u, v);
 #pragma unroll
     for (int i = 0; i < 3; i++) u[i] = axpy<kExact>(s.delta, v[i], u[i]);
-    if (slot >= 0) apply_bc(bc, s.delta, u, v);
+    if (slot >= 0) apply_bc(bc, s.delta, s.time, a.ex, n, u, v);
   }
 #pragma unroll
   for (int i = 0; i < 3; i++) {
@@ -150,7 +230,8 @@ cudaError_t launch_advance_base(int* step_base, int k, cudaStream_t stream)
 }
 
 __global__ void k_apply_bc(int N, long ld_n, const int* __restrict__ bc_slot, const NodeBC* __restrict__ bcs,
-                           double delta, const double* __restrict__ u, double* __restrict__ v)
+                           double delta, double time, BcExprTable ex, const double* __restrict__ u,
+                           double* __restrict__ v)
 {
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= N) return;
@@ -162,16 +243,16 @@ __global__ void k_apply_bc(int N, long ld_n, const int* __restrict__ bc_slot, co
     uu[i] = u[i * ld_n + n];
     vv[i] = v[i * ld_n + n];
   }
-  apply_bc(bcs[slot], delta, uu, vv);
+  apply_bc(bcs[slot], delta, time, ex, n, uu, vv);
 #pragma unroll
   for (int i = 0; i < 3; i++) v[i * ld_n + n] = vv[i];
 }
 
-cudaError_t launch_apply_bc(int N, long ld_n, const int* bc_slot, const NodeBC* bcs, double delta, const double* u,
-                            double* v, cudaStream_t stream)
+cudaError_t launch_apply_bc(int N, long ld_n, const int* bc_slot, const NodeBC* bcs, double delta, double time,
+                            const BcExprTable& ex, const double* u, double* v, cudaStream_t stream)
 {
   if (N == 0) return cudaSuccess;
-  k_apply_bc<<<grid_for(N, 256), 256, 0, stream>>>(N, ld_n, bc_slot, bcs, delta, u, v);
+  k_apply_bc<<<grid_for(N, 256), 256, 0, stream>>>(N, ld_n, bc_slot, bcs, delta, time, ex, u, v);
   return cudaGetLastError();
 }
 

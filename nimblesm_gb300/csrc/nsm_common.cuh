@@ -54,6 +54,7 @@ __host__ __device__ constexpr int sym_slot(int i, int k)
 struct StepSched {
   double delta;
   double half;
+  double time;  // time_current of the step (boundary-condition expressions)
   int    is_output;
   int    pad;
 };
@@ -61,12 +62,34 @@ struct StepSched {
 // Boundary-condition action on one node, the last one in deck order per
 // component (each BC line overwrites the velocity component it names,
 // src/nimble_boundary_condition_manager.h:136-217).  kind: 0 none,
-// 1 prescribed velocity, 2 prescribed displacement.
+// 1 prescribed velocity, 2 prescribed displacement.  expr: -1 for the
+// constant value[k], else the index of the expression program f(x, y, z, t)
+// that gives it.
 struct NodeBC {
   int8_t kind[3];
-  int8_t pad[5];
+  int8_t expr[3];
+  int8_t pad[2];
   double value[3];
 };
+
+// Postfix programs of boundary-condition expressions (bc_expression.cu).
+// Constants and variables push; unary operations replace the top; binary
+// ones pop one; kExSelect pops two (condition, if-true, if-false).
+enum ExprCode : int {
+  kExConst, kExX, kExY, kExZ, kExT,
+  kExAdd, kExSub, kExMul, kExDiv, kExMod, kExPow,
+  kExNeg, kExSin, kExCos, kExTan, kExErf, kExExp, kExLog, kExAbs, kExAsin, kExAcos, kExAtan, kExSqrt, kExCbrt,
+  kExErfc, kExCeil, kExRound, kExFloor, kExLog10, kExNot,
+  kExGt, kExGe, kExLt, kExLe, kExEq, kExAnd, kExOr, kExXor,
+  kExSelect
+};
+struct ExprOp {
+  int    code;
+  int    pad;
+  double c;  // kExConst
+};
+constexpr int kExprStack = 16;  // operand stack of the evaluators; deeper programs are refused
+__host__ __device__ constexpr bool expr_is_unary(int code) { return code >= kExNeg && code <= kExNot; }
 
 inline int grid_for(long n, int block) { return (int)((n + block - 1) / block); }
 

@@ -3,6 +3,9 @@
 // element field is planes of ld_e entries, one plane per component).
 #pragma once
 
+#include <string>
+#include <vector>
+
 #include "nsm_common.cuh"
 
 // Device status word bits (read back by the host, returned as C status codes).
@@ -104,6 +107,22 @@ cudaError_t launch_ip_identity(int E, long ld_e, void* ip, int ip_is_float, cuda
 
 // Node kernel: the end of step s (gather f_int, a = f/m, v += half*a, output
 // BCs) fused with the start of step s+1 (v += half*a, BCs, u += delta*v, BCs).
+// The expression programs of a model's boundary conditions and the node
+// coordinates they read (x, y, z of the reference configuration).
+struct BcExprTable {
+  const ExprOp* code;   // programs, concatenated
+  const int*    start;  // [programs + 1] first op of each
+  const double* X;      // [3][ld_n]
+  long          ld_n;
+};
+
+// Boundary-condition expressions (bc_expression.cu): the reference's grammar
+// to a postfix program appended to `code` (an error message, or empty); one
+// operation and a whole program evaluated on the host.
+std::string compile_bc_expression(const std::string& text, std::vector<ExprOp>& code);
+double      apply_host(int code, double a, double b);
+double      eval_bc_expression_host(const ExprOp* code, int count, double x, double y, double z, double t);
+
 struct NodeArgs {
   int               N;        // nodes [n_begin, N) are updated by this launch
   int               n_begin;
@@ -133,6 +152,7 @@ struct NodeArgs {
   const double*     closure;  // or null
   int               closure_first, num_exact;
   const int*        node_off; // [num_groups + 1] first node of each sample
+  BcExprTable       ex;       // boundary-condition expressions
 };
 
 cudaError_t launch_node_update(const NodeArgs& a, cudaStream_t stream);
@@ -140,8 +160,8 @@ cudaError_t launch_advance_base(int* step_base, int k, cudaStream_t stream);
 
 // Kinematic conditions alone (ApplyKinematicConditions with delta_t), and
 // initial conditions (velocity values).
-cudaError_t launch_apply_bc(int N, long ld_n, const int* bc_slot, const NodeBC* bcs, double delta, const double* u,
-                            double* v, cudaStream_t stream);
+cudaError_t launch_apply_bc(int N, long ld_n, const int* bc_slot, const NodeBC* bcs, double delta, double time,
+                            const BcExprTable& ex, const double* u, double* v, cudaStream_t stream);
 
 // Energies: kinetic 1/2 m v.v (per-node) and internal sum det J0 W(F) per ip;
 // two-pass deterministic sums into out[0], out[1].

@@ -45,6 +45,7 @@ struct BcLine {
   int              kind, component;
   double           value;
   std::vector<int> nodes;
+  int              expr = -1;  // expression program giving the value, or -1
 };
 
 }  // namespace
@@ -94,6 +95,10 @@ struct nsm_model {
 
   std::vector<BcLine> bcs;
   bool                bcs_dirty = true;
+  std::vector<nsm::ExprOp> expr_code;           // expression programs, concatenated
+  std::vector<int>         expr_start{0};       // [programs + 1]
+  nsm::ExprOp*             d_expr_code = nullptr;
+  int*                     d_expr_start = nullptr;
   int*                d_bc_slot = nullptr;
   NodeBC*             d_bcs = nullptr;
   int*                d_ibc_slot = nullptr;
@@ -140,7 +145,7 @@ void free_all(nsm_model* m)
                   m->d_uf,   m->d_fe,   m->d_status,   m->d_step_base, m->d_scratch, m->d_stage,  m->d_out,   m->d_bc_slot,
                   m->d_bcs,  m->d_ibc_slot, m->d_ibcs,     m->d_sched, m->d_group_out, m->d_elem_group,
                   m->d_node_group, m->d_elem_off, m->d_mats, m->d_fallbacks, m->d_node_off, m->d_closure,
-                  m->d_stage_out};
+                  m->d_stage_out, m->d_expr_code, m->d_expr_start};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (cudaStream_t s : m->hp_stream)
@@ -186,11 +191,13 @@ int upload_bcs(nsm_model* m)
           slot[n] = (int)table.size();
           NodeBC z;
           std::memset(&z, 0, sizeof(z));
+          z.expr[0] = z.expr[1] = z.expr[2] = -1;
           table.push_back(z);
         }
         NodeBC& t          = table[slot[n]];
         t.kind[b.component]  = (int8_t)(initial ? 1 : (b.kind == NSM_BC_PRESCRIBED_VELOCITY ? 1 : 2));
         t.value[b.component] = b.value;
+        t.expr[b.component]  = (int8_t)b.expr;
       }
     }
     int*&    d_slot = pass == 0 ? m->d_bc_slot : m->d_ibc_slot;
@@ -206,6 +213,19 @@ int upload_bcs(nsm_model* m)
     if (m->N > 0)
       NSM_CUDA(cudaMemcpyAsync(d_slot, slot.data(), sizeof(int) * m->N, cudaMemcpyHostToDevice, m->stream));
     NSM_CUDA(cudaStreamSynchronize(m->stream));  // host vectors go out of scope
+  }
+  // expression programs
+  if (m->d_expr_code) cudaFree(m->d_expr_code);
+  if (m->d_expr_start) cudaFree(m->d_expr_start);
+  m->d_expr_code  = nullptr;
+  m->d_expr_start = nullptr;
+  if (!m->expr_code.empty()) {
+    NSM_CUDA(cudaMalloc(&m->d_expr_code, sizeof(nsm::ExprOp) * m->expr_code.size()));
+    NSM_CUDA(cudaMalloc(&m->d_expr_start, sizeof(int) * m->expr_start.size()));
+    NSM_CUDA(cudaMemcpy(m->d_expr_code, m->expr_code.data(), sizeof(nsm::ExprOp) * m->expr_code.size(),
+                        cudaMemcpyHostToDevice));
+    NSM_CUDA(cudaMemcpy(m->d_expr_start, m->expr_start.data(), sizeof(int) * m->expr_start.size(),
+                        cudaMemcpyHostToDevice));
   }
   m->bcs_dirty = false;
   // captured graphs hold the old table's address
@@ -256,6 +276,11 @@ nsm::ElementArgs element_args(nsm_model* m, int k)
   return a;
 }
 
+nsm::BcExprTable expr_table(const nsm_model* m)
+{
+  return nsm::BcExprTable{m->d_expr_code, m->d_expr_start, m->d_X, m->ld_n};
+}
+
 nsm::NodeArgs node_args(nsm_model* m, int k_post, int k_pre, int gather_only)
 {
   nsm::NodeArgs a;
@@ -286,6 +311,7 @@ nsm::NodeArgs node_args(nsm_model* m, int k_post, int k_pre, int gather_only)
   a.closure_first = m->closure_first;
   a.num_exact     = m->num_exact;
   a.node_off      = m->d_node_off;
+  a.ex            = expr_table(m);
   return a;
 }
 
@@ -754,6 +780,35 @@ int nsm_add_boundary_condition(nsm_model* m, int kind, int component, double val
   return NSM_OK;
 }
 
+int nsm_add_boundary_condition_expression(nsm_model* m, int kind, int component, const char* expression,
+                                          const int* nodes, int count)
+{
+  if (!m || !expression || (count > 0 && !nodes)) return fail(NSM_ERR_INVALID_ARGUMENT, "null argument");
+  if (kind < NSM_BC_INITIAL_VELOCITY || kind > NSM_BC_PRESCRIBED_DISPLACEMENT)
+    return fail(NSM_ERR_INVALID_ARGUMENT, "unknown boundary condition kind");
+  if (component < 0 || component > 2) return fail(NSM_ERR_INVALID_ARGUMENT, "unknown coordinate");
+  if ((int)m->expr_start.size() - 1 >= 127) return fail(NSM_ERR_INVALID_ARGUMENT, "more than 127 expressions");
+  for (int i = 0; i < count; i++)
+    if (nodes[i] < 0 || nodes[i] >= m->N) return fail(NSM_ERR_INVALID_ARGUMENT, "node set entry out of range");
+  const std::string err = nsm::compile_bc_expression(expression, m->expr_code);
+  if (!err.empty()) return fail(NSM_ERR_INVALID_ARGUMENT, ("boundary condition expression: " + err).c_str());
+  m->expr_start.push_back((int)m->expr_code.size());
+  BcLine b{kind, component, 0.0, std::vector<int>(nodes, nodes + count), (int)m->expr_start.size() - 2};
+  m->bcs.push_back(std::move(b));
+  m->bcs_dirty = true;
+  return NSM_OK;
+}
+
+int nsm_bc_expression_eval(const char* expression, double x, double y, double z, double t, double* value)
+{
+  if (!expression || !value) return fail(NSM_ERR_INVALID_ARGUMENT, "null argument");
+  std::vector<nsm::ExprOp> code;
+  const std::string        err = nsm::compile_bc_expression(expression, code);
+  if (!err.empty()) return fail(NSM_ERR_INVALID_ARGUMENT, ("boundary condition expression: " + err).c_str());
+  *value = nsm::eval_bc_expression_host(code.data(), (int)code.size(), x, y, z, t);
+  return NSM_OK;
+}
+
 int nsm_compute_lumped_mass(nsm_model* m, double* mass)
 {
   if (!m) return fail(NSM_ERR_INVALID_ARGUMENT, "null model");
@@ -778,7 +833,9 @@ int nsm_apply_initial_conditions(nsm_model* m)
   NSM_CUDA(cudaSetDevice(m->device));
   int r = upload_bcs(m);
   if (r) return r;
-  if (m->d_ibcs) NSM_CUDA(nsm::launch_apply_bc(m->N, m->ld_n, m->d_ibc_slot, m->d_ibcs, 0.0, m->d_u, m->d_v, m->stream));
+  if (m->d_ibcs)
+    NSM_CUDA(nsm::launch_apply_bc(m->N, m->ld_n, m->d_ibc_slot, m->d_ibcs, 0.0, 0.0, expr_table(m), m->d_u, m->d_v,
+                                  m->stream));
   return NSM_OK;
 }
 
@@ -789,7 +846,8 @@ int nsm_apply_kinematic_conditions(nsm_model* m, double t_cur, double t_prev)
   int r = upload_bcs(m);
   if (r) return r;
   if (m->d_bcs)
-    NSM_CUDA(nsm::launch_apply_bc(m->N, m->ld_n, m->d_bc_slot, m->d_bcs, t_cur - t_prev, m->d_u, m->d_v, m->stream));
+    NSM_CUDA(nsm::launch_apply_bc(m->N, m->ld_n, m->d_bc_slot, m->d_bcs, t_cur - t_prev, t_cur, expr_table(m), m->d_u,
+                                  m->d_v, m->stream));
   return NSM_OK;
 }
 
@@ -1053,7 +1111,7 @@ int nsm_begin_ensemble(nsm_model* m, double initial_time, const double* final_ti
   // per-sample schedules as src/integrators/explicit_time_integrator.cc:130-199
   // forms them, laid out [step][sample]
   const int S = m->S;
-  m->h_sched.assign((size_t)(num_steps > 0 ? num_steps : 1) * S, StepSched{0, 0, 0, 0});
+  m->h_sched.assign((size_t)(num_steps > 0 ? num_steps : 1) * S, StepSched{0, 0, 0, 0, 0});
   m->h_time.assign((size_t)(num_steps + 1), initial_time);
   for (int g = 0; g < S; g++) {
     double t_cur = initial_time, t_prev = initial_time;
@@ -1064,6 +1122,7 @@ int nsm_begin_ensemble(nsm_model* m, double initial_time, const double* final_ti
       StepSched& q = m->h_sched[(size_t)s * S + g];
       q.delta      = t_cur - t_prev;
       q.half       = 0.5 * q.delta;
+      q.time       = t_cur;
       q.is_output  = (output_frequency != 0 && (s % output_frequency == 0 || s == num_steps - 1)) ? 1 : 0;
       if (g == 0) m->h_time[s + 1] = t_cur;
     }

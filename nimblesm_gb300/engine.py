@@ -69,6 +69,8 @@ SIGNATURES = {
                                 _dp, C.POINTER(_Options), C.POINTER(_vp)]),
     "nsm_destroy": (C.c_int, [_vp]),
     "nsm_add_boundary_condition": (C.c_int, [_vp, C.c_int, C.c_int, C.c_double, _ip, C.c_int]),
+    "nsm_add_boundary_condition_expression": (C.c_int, [_vp, C.c_int, C.c_int, C.c_char_p, _ip, C.c_int]),
+    "nsm_bc_expression_eval": (C.c_int, [C.c_char_p, C.c_double, C.c_double, C.c_double, C.c_double, _dp]),
     "nsm_compute_lumped_mass": (C.c_int, [_vp, _dp]),
     "nsm_critical_time_step": (C.c_int, [_vp, _dp]),
     "nsm_apply_initial_conditions": (C.c_int, [_vp]),
@@ -146,6 +148,25 @@ def _check(rc):
         raise EngineError(rc, library().nsm_last_error().decode())
 
 
+def _add_bc(lib, h, bc, nodes):
+    """One boundary-condition line over its (global) node ids."""
+    if bc.expression is not None:
+        _check(lib.nsm_add_boundary_condition_expression(h, bc.kind, bc.component, bc.expression.encode(),
+                                                         nodes.ctypes.data_as(_ip), len(nodes)))
+    else:
+        _check(lib.nsm_add_boundary_condition(h, bc.kind, bc.component, bc.value, nodes.ctypes.data_as(_ip),
+                                              len(nodes)))
+
+
+def bc_expression_eval(expression, x=0.0, y=0.0, z=0.0, t=0.0):
+    """One host evaluation of a boundary-condition expression as the engine
+    parses it (nsm_bc_expression_eval)."""
+    v = C.c_double()
+    _check(library().nsm_bc_expression_eval(expression.encode(), float(x), float(y), float(z), float(t),
+                                           C.byref(v)))
+    return v.value
+
+
 def _d(a):
     return a.ctypes.data_as(_dp)
 
@@ -216,8 +237,7 @@ class Model:
                 if bc.node_set not in p.node_sets:
                     continue  # the reference drops lines naming an absent node set
                 nodes = np.ascontiguousarray(np.asarray(p.node_sets[bc.node_set]) + no[g], dtype=np.int32)
-                _check(lib.nsm_add_boundary_condition(h, bc.kind, bc.component, bc.value,
-                                                      nodes.ctypes.data_as(_ip), len(nodes)))
+                _add_bc(lib, h, bc, nodes)
 
     def close(self):
         if getattr(self, "_h", None):
@@ -516,8 +536,7 @@ class UqModel(Model):
                 if bc.kind == BC_PRESCRIBED_DISPLACEMENT and t > 0:
                     continue
                 nodes = np.ascontiguousarray(np.asarray(problem.node_sets[bc.node_set]) + no[t], dtype=np.int32)
-                _check(lib.nsm_add_boundary_condition(h, bc.kind, bc.component, bc.value,
-                                                      nodes.ctypes.data_as(_ip), len(nodes)))
+                _add_bc(lib, h, bc, nodes)
 
     def trajectories(self, label):
         """A nodal vector field of every trajectory: [trajectories, N, 3]

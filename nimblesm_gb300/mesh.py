@@ -33,31 +33,47 @@ CORNER_SIGNS = np.array(
 
 @dataclass
 class BoundaryCondition:
-    """One boundary-condition line of the input deck with a constant magnitude."""
+    """One boundary-condition line of the input deck: a constant magnitude, or
+    an expression f(x, y, z, t) of the node's reference coordinates and the
+    time (the quoted form)."""
     kind: int
     node_set: str
     component: int
     value: float
+    expression: str | None = None
 
     @staticmethod
     def parse(line: str) -> "BoundaryCondition":
-        """Parses "<kind> <nodeset> <x|y|z> <value>" as
-        BoundaryCondition::Initialize does (src/nimble_boundary_condition.cc:65-144);
-        expression magnitudes (quoted) are not supported and raise."""
-        if '"' in line:
-            raise ValueError("expression boundary conditions are not supported: " + line)
-        parts = line.split()
-        if len(parts) != 4:
-            raise ValueError("malformed boundary condition: " + line)
-        kind, ns, comp, val = parts
+        """Parses "<kind> <nodeset> <x|y|z> <value>" or "<kind> <nodeset>
+        <x|y|z> "<expression>"" as BoundaryCondition::Initialize does
+        (src/nimble_boundary_condition.cc:65-144): two quotes make the text
+        between the first and the last an expression."""
+        quotes = line.count('"')
+        if quotes not in (0, 2):
+            raise ValueError("illegal number of quotes in boundary condition: " + line)
+        expression = None
+        if quotes == 2:
+            expression = line[line.index('"') + 1: line.rindex('"')]
+            parts = line[: line.index('"')].split()
+            if len(parts) != 3:
+                raise ValueError("malformed boundary condition: " + line)
+            kind, ns, comp = parts
+            val = 0.0
+        else:
+            parts = line.split()
+            if len(parts) != 4:
+                raise ValueError("malformed boundary condition: " + line)
+            kind, ns, comp, val = parts
         if kind not in _BC_KINDS:
             raise ValueError("unknown boundary condition type: " + kind)
         if comp.lower() not in _COMPONENTS:
             raise ValueError("unknown coordinate: " + comp)
-        return BoundaryCondition(_BC_KINDS[kind], ns, _COMPONENTS[comp.lower()], float(val))
+        return BoundaryCondition(_BC_KINDS[kind], ns, _COMPONENTS[comp.lower()], float(val), expression)
 
     def line(self) -> str:
         kind = {v: k for k, v in _BC_KINDS.items()}[self.kind]
+        if self.expression is not None:
+            return f'{kind} {self.node_set} {"xyz"[self.component]} "{self.expression}"'
         return f"{kind} {self.node_set} {'xyz'[self.component]} {self.value!r}"
 
 
@@ -121,6 +137,8 @@ class Problem:
         for bc in self.bcs:
             if bc.node_set not in self.node_sets:
                 continue
+            if bc.expression is not None:
+                raise ValueError("constant boundary magnitudes only: " + bc.line())
             ids = np.asarray(self.node_sets[bc.node_set], dtype=np.int32)
             kinds.append(bc.kind)
             comps.append(bc.component)

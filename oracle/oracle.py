@@ -144,6 +144,7 @@ def ref():
         lib.nimref_element.argtypes = [_dp, _dp, C.c_double, C.c_double, C.c_double, _dp, _dp, _dp]
         lib.nimref_stress.argtypes = [C.c_int, _dp, C.c_double, C.c_double, _dp]
         lib.nimref_volume_average.argtypes = [_dp, C.c_int, _dp, _dp, _dp]
+        lib.nimref_eval_expression.argtypes = [C.c_char_p, C.c_double, C.c_double, C.c_double, C.c_double, _dp]
         lib.nimref_last_error.restype = C.c_char_p
         _ref = lib
     return _ref
@@ -248,6 +249,16 @@ def continue_port(problem, u, v, a, t0, dt, num_steps, threads):
     if rc != 0:
         raise RuntimeError(f"oracle continue failed ({rc})")
     return secs.value
+
+
+def ref_eval_expression(text, x, y, z, t):
+    """A boundary-condition expression evaluated by the reference's parser
+    (oracle/_ref): its value, or a ValueError with the reference's message."""
+    lib = ref()
+    v = C.c_double(0.0)
+    if lib.nimref_eval_expression(text.encode(), float(x), float(y), float(z), float(t), C.byref(v)) != 0:
+        raise ValueError(lib.nimref_last_error().decode())
+    return v.value
 
 
 def run_ref_outputs(problem, final_time, num_steps, output_frequency=0, with_ip=True):

@@ -25,6 +25,7 @@
 #include "nimble_boundary_condition_manager.h"
 #include "nimble_data_manager.h"
 #include "nimble_element.h"
+#include "nimble_expression_parser.h"
 #include "nimble_genesis_mesh.h"
 #include "nimble_material.h"
 #include "nimble_material_factory.h"
@@ -592,6 +593,25 @@ nimref_volume_average(const double* x_cur, int nq, const double* q, double* volu
     return 0;
   } catch (std::exception const& ex) {
     g_last_error = ex.what();
+    return -1;
+  }
+}
+
+// A boundary-condition expression evaluated by the reference's own parser
+// (ExpressionParsing::BoundaryConditionFunctor,
+// src/nimble_expression_parser.h:697-800) at (x, y, z, t).
+int
+nimref_eval_expression(const char* text, double x, double y, double z, double t, double* value)
+{
+  try {
+    ExpressionParsing::BoundaryConditionFunctor f{std::string(text)};
+    *value = f.eval(x, y, z, t);
+    return 0;
+  } catch (std::exception const& ex) {
+    g_last_error = ex.what();
+    return -1;
+  } catch (...) {
+    g_last_error = "unknown exception";
     return -1;
   }
 }

@@ -313,8 +313,84 @@ def ref_gold_rerun():
         print("wrote ref rerun", name, out_steps)
 
 
+# Boundary-condition expressions (written for these tests; they cover the
+# reference grammar: precedence, associativity, unary minus, exponents,
+# functions, constants, conditions) and points (x, y, z, t).
+BC_EXPRESSIONS = [
+    "1.5e-3 * t", "2.0*x - 0.5*y + z/4", "x^2 + y^3 - z^-2", "sqrt(x*x + y*y)", "exp(-t*1e5) * sin(2*pi*x)",
+    "t < 5e-6 ? 1e3*t : 5e-3", "(x > 0.5 & y <= 0.5) | z == 0.25 ? 1 : -1",
+    "abs(x - 0.5) + floor(y*3) + ceil(z*2.5) + round(x*7.3)", "log(1 + x) + log10(10 + y) + cbrt(z + 2)",
+    "atan(x) + asin(y/2) + acos(z/3)", "erf(x) + erfc(y) + tan(z/2)", "10 % 4 + 1", "x % 0.3 + 1", "2^3^2",
+    "-x - -y", "-(x + y) * -z", "e^x - tau*y + pi", "3*x/4*y/2", "x - y - z + t", "1e-3*sin(t*1.0e6)*x",
+    "TAU*X + Sin(Y)", "((x))+(((y)))", "x*-2 + 1", "2e-3*x", "1.e2*y", ".5*z", "x ^ 0.5", "x^(1/3)",
+    "!(x > 0.5) ? x : y", "x > 0.2 ^ y > 0.3 ? 1 : 0", "t >= 2e-6 ? (t <= 8e-6 ? 2*t : 3*t) : t/2",
+    "8/2/2", "1 - 2 - 3", "x*y*z*t*1e6", "  ( x + 1 ) * ( y - 1 )  ", "exp(log(x+1)/2)", "-2^2", "(-2)^2",
+    "x^2.5", "100*t - 0.001", "5 - -3", "sin(x)^2 + cos(x)^2", "1e-3 - x", "0.25*(1 - x)*(1 + y)",
+]
+# refused by the reference: an unknown name, an exponent's sign taken for an
+# operator, an unclosed call, an unknown function, two operands
+BC_EXPRESSIONS_BAD = ["a+1", "2*1e+5", "x - 1e-3", "sin(x", "foo(x)", "x y"]
+BC_POINTS = [(0.0, 0.0, 0.25, 0.0), (0.3, 0.7, 0.25, 1.0e-6), (0.75, 0.2, 0.5, 5.0e-6), (1.0, 1.0, 1.0, 9.5e-6),
+             (0.5, 0.5, 0.75, 2.0e-6), (0.125, 0.875, 0.375, 8.0e-6)]
+
+
+def ref_bc_expressions_fixture():
+    """The reference parser's values of BC_EXPRESSIONS at BC_POINTS, and the
+    expressions it refuses."""
+    vals = np.array([[O.ref_eval_expression(e, *pt) for pt in BC_POINTS] for e in BC_EXPRESSIONS])
+    for e in BC_EXPRESSIONS_BAD:
+        try:
+            O.ref_eval_expression(e, *BC_POINTS[1])
+            raise RuntimeError("the reference parsed " + e)
+        except ValueError:
+            pass
+    np.savez_compressed(os.path.join(HERE, "ref_bc_expressions.npz"), expressions=np.array(BC_EXPRESSIONS),
+                        bad=np.array(BC_EXPRESSIONS_BAD), points=np.array(BC_POINTS), values=vals)
+    print("wrote bc expressions", vals.shape)
+
+
+# A cube driven by expression conditions only (no initial velocity field):
+# time- and position-dependent prescribed displacement and velocity on the
+# bottom face, initial and prescribed velocity on the top face.
+BC_EXPRESSION_RUN = [
+    'initial_velocity nodelist_2 x "25.0*x*y"',
+    'initial_velocity nodelist_2 z "-40.0*(1 + 0.5*sin(pi*x))"',
+    'prescribed_displacement nodelist_1 z "1.0e-4*sin(t*2.0e5)*(1 + x*y)"',
+    'prescribed_displacement nodelist_1 x "0.0"',
+    'prescribed_velocity nodelist_1 y "t < 4.0e-6 ? 2.5e5*t*(1 - x) : 1.0 - x"',
+    'prescribed_velocity nodelist_2 y "x > 0.5 ? 0.5 : -0.5"',
+]
+
+
+def bc_expression_problem(n=6, seed=3):
+    p = cube_problem(n, jitter=0.2, seed=seed)
+    p.v_init = None
+    p.bcs = [BoundaryCondition.parse(line) for line in BC_EXPRESSION_RUN]
+    return p
+
+
+def ref_bc_expression_run_fixture(steps=300, output_frequency=50):
+    p = bc_expression_problem()
+    dt = 0.5 * critical_time_step(p)
+    outs = O.run_ref_outputs(p, steps * dt, steps, output_frequency)
+    fx = {"steps": steps, "output_frequency": output_frequency, "final_time": steps * dt,
+          "bc_lines": np.array(BC_EXPRESSION_RUN)}
+    for k in ("u", "v", "a", "f_int"):
+        fx[k] = np.stack([o[k] for o in outs])
+    fx["F"], fx["sigma"] = outs[-1]["F"], outs[-1]["sigma"]  # the last output's point data
+    np.savez_compressed(os.path.join(HERE, "ref_bc_expression_cube6.npz"), **fx)
+    print("wrote bc expression run", fx["u"].shape)
+
+
+GENERATORS = {"bc_expressions": lambda: (ref_bc_expressions_fixture(), ref_bc_expression_run_fixture())}
+
+
 if __name__ == "__main__":
     O.build(ref=True)
+    if len(sys.argv) > 1:  # only the named fixture groups
+        for name in sys.argv[1:]:
+            GENERATORS[name]()
+        sys.exit(0)
     for deck in GOLD_DECKS:
         gold_fixture(*deck)
     ref_points_fixture()

@@ -20,6 +20,50 @@ __device__ __forceinline__ void store_vec(double* dst, const double* v, int n)
   for (int k = 0; k < n; k += 2) *reinterpret_cast<double2*>(dst + k) = make_double2(v[k], v[k + 1]);
 }
 
+// Warp-cooperative stores.  A thread's point record (64 or 128 B) and its
+// element forces (96 or 192 B) are contiguous, and so are those of the 32
+// consecutive elements of a warp; stored lane by lane, each store instruction
+// would scatter 16-byte pieces a record apart, which HBM takes at half the
+// rate of contiguous writes.  Instead the warp passes its 32 blocks through a
+// shared-memory tile and each instruction writes 512 contiguous bytes.  The
+// tile slots are swizzled (4 and 8 chunks per block) or padded (6 and 12) so
+// that neither the per-lane writes nor the transposed reads conflict on banks.
+template <int kChunks>
+__device__ __forceinline__ int tile_slot(int row, int c)
+{
+  if constexpr (kChunks == 4) return row * 4 + (c ^ ((row >> 1) & 3));
+  else if constexpr (kChunks == 8) return row * 8 + (c ^ (row & 7));
+  else return row * (kChunks + 1) + c;
+}
+template <int kChunks>
+__host__ __device__ constexpr int tile_chunks() { return 32 * (kChunks == 4 || kChunks == 8 ? kChunks : kChunks + 1); }
+
+__device__ __forceinline__ uint4 pack16(const float* v, int c)
+{
+  return make_uint4(__float_as_uint(v[4 * c]), __float_as_uint(v[4 * c + 1]), __float_as_uint(v[4 * c + 2]),
+                    __float_as_uint(v[4 * c + 3]));
+}
+__device__ __forceinline__ uint4 pack16(const double* v, int c)
+{
+  const unsigned long long a = __double_as_longlong(v[2 * c]), b = __double_as_longlong(v[2 * c + 1]);
+  return make_uint4((unsigned)a, (unsigned)(a >> 32), (unsigned)b, (unsigned)(b >> 32));
+}
+
+// dst: the first lane's block; all 32 lanes of the warp take part.
+template <int kChunks, typename T>
+__device__ __forceinline__ void warp_store(uint4* __restrict__ dst, const T* v, uint4* tile, int lane)
+{
+  __syncwarp();  // the tile's previous contents have been read
+#pragma unroll
+  for (int c = 0; c < kChunks; c++) tile[tile_slot<kChunks>(lane, c)] = pack16(v, c);
+  __syncwarp();
+#pragma unroll
+  for (int k = 0; k < kChunks; k++) {
+    const int j = k * 32 + lane;
+    dst[j]      = tile[tile_slot<kChunks>(j / kChunks, j % kChunks)];
+  }
+}
+
 // J > 0 without the FP64 pipe: the sign and magnitude bits of an IEEE number
 // order like a signed integer (a NaN J passes here and is caught as a
 // non-finite force).
@@ -198,6 +242,15 @@ __device__ __forceinline__ void element_work(const ElementArgs& a, const int e, 
   T*      rec = reinterpret_cast<T*>(a.ip) + (size_t)e * kIpRecord;
   const bool store =
       a.store_ip || (a.sched != nullptr && a.sched[(long)(*a.step_base + a.k) * a.num_groups].is_output);
+  // a warp of 32 consecutive elements stores through its tile; a partial warp lane by lane
+  constexpr int kRecChunks = kIpRecord * (int)sizeof(T) / 16, kForceChunks = 24 * (int)sizeof(T) / 16;
+  constexpr int kTile      = tile_chunks<kRecChunks>() > tile_chunks<kForceChunks>() ? tile_chunks<kRecChunks>()
+                                                                                       : tile_chunks<kForceChunks>();
+  __shared__ uint4 tiles[4][kTile];  // blocks of at most 128 threads
+  const int        lane   = threadIdx.x & 31;
+  const long       e0     = (long)e - lane;  // the warp's elements are e0 .. e0 + 31
+  const bool       whole  = e0 + 32 <= a.E;
+  uint4*           tile   = tiles[(threadIdx.x >> 5) & 3];
 
 #pragma unroll
   for (int p = 0; p < 8; p++) {
@@ -248,7 +301,11 @@ __device__ __forceinline__ void element_work(const ElementArgs& a, const int e, 
 #pragma unroll
       for (int q = 0; q < 6; q++) r[9 + q] = sig[q];
       r[15] = T(0);
-      store_vec(rec + (size_t)p * ld_e * kIpRecord, r, kIpRecord);
+      if (whole)
+        warp_store<kRecChunks>(reinterpret_cast<uint4*>(reinterpret_cast<T*>(a.ip) + ((size_t)p * ld_e + e0) * kIpRecord),
+                               r, tile, lane);
+      else
+        store_vec(rec + (size_t)p * ld_e * kIpRecord, r, kIpRecord);
     }
     // Q[d][i] = sum_k adj(J_x)[d][k] sigma[k][i] = sum_k cof(J_x)[k][d] sigma[k][i],
     // summed over the two points of each sign pair (the first assigns)
@@ -275,7 +332,10 @@ __device__ __forceinline__ void element_work(const ElementArgs& a, const int e, 
       fv[n * 3 + i] = f[n][i];
       finite        = finite && isfinite(f[n][i]);
     }
-  store_vec(reinterpret_cast<T*>(a.fe) + (size_t)e * 24, fv, 24);
+  if (whole)
+    warp_store<kForceChunks>(reinterpret_cast<uint4*>(reinterpret_cast<T*>(a.fe) + (size_t)e0 * 24), fv, tile, lane);
+  else
+    store_vec(reinterpret_cast<T*>(a.fe) + (size_t)e * 24, fv, 24);
   if (bad || !finite) atomicOr(a.status, (bad ? NSM_STATUS_BAD_JACOBIAN : 0) | (finite ? 0 : NSM_STATUS_NONFINITE));
 }
 

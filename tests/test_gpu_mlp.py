@@ -114,7 +114,7 @@ def test_fused_forces_match_the_material(mlp):
     p = cube_problem(8, jitter=0.2, seed=6)
     rng = np.random.default_rng(8)
     u = rng.normal(0, 2e-4, size=(p.num_nodes, 3))
-    f = {}
+    f, F = {}, {}
     for form in ("plain", "mlp"):
         m = E.Model(p, precision="fp32")
         if form == "mlp":
@@ -122,7 +122,10 @@ def test_fused_forces_match_the_material(mlp):
         m.SetVectorNodeData("displacement", u)
         m.ComputeInternalForce()
         f[form] = m.GetVectorNodeData("internal_force")
+        F[form] = m.GetIntegrationPointData()[0]
         m.close()
+    # each point's F record lands where the plain kernel puts it (FP32 rounding apart)
+    assert rel(F["mlp"], F["plain"]) < 1e-6, rel(F["mlp"], F["plain"])
     assert rel(f["mlp"], f["plain"]) < 2e-3, rel(f["mlp"], f["plain"])
     scale = np.abs(f["plain"]).max()
     assert np.abs(f["mlp"] - f["plain"]).max() < 5e-3 * scale

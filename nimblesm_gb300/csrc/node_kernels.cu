@@ -90,15 +90,15 @@ __device__ __noinline__ double eval_bc_expression(const BcExprTable& ex, int pro
 // ApplyKinematicBC for the explicit scheme
 // (src/nimble_boundary_condition_manager.h:136-217): prescribed velocity sets
 // v; prescribed displacement sets v = (d - u) / delta when delta > 0.  The
-// magnitude is the line's constant or its expression at the node's reference
-// coordinates and time_current.
-__device__ __forceinline__ void apply_bc(const NodeBC& bc, double delta, double time, const BcExprTable& ex, int n,
-                                         const double u[3], double v[3])
+// magnitude is the line's constant or its expression's value at the node's
+// reference coordinates and time_current (`ev`, evaluated beforehand).
+__device__ __forceinline__ void apply_bc(const NodeBC& bc, double delta, const double* ev, const double u[3],
+                                         double v[3])
 {
 #pragma unroll
   for (int k = 0; k < 3; k++) {
     if (bc.kind[k] == 0 || (bc.kind[k] == 2 && !(delta > 0.0))) continue;
-    const double value = bc.expr[k] < 0 ? bc.value[k] : eval_bc_expression(ex, bc.expr[k], n, time);
+    const double value = bc.expr[k] < 0 ? bc.value[k] : ev[k];
     if (bc.kind[k] == 1) {
       v[k] = value;
     } else {
@@ -121,14 +121,32 @@ __device__ __forceinline__ void gather_force(const NodeArgs& a, int n, double f[
 {
   const TF* fe    = reinterpret_cast<const TF*>(a.fe);
   TF        fs[3] = {TF(0), TF(0), TF(0)};
-  for (int k = a.node_ptr[n]; k < a.node_ptr[n + 1]; k++) {
+  const int k0 = __ldg(&a.node_ptr[n]), k1 = __ldg(&a.node_ptr[n + 1]);
+  // the first 8 incidences (all of them at a hex mesh's interior node): every
+  // load issued before the first sum, the sums in the same order as below
+  constexpr int kFirst = 8;
+  int           ec[kFirst];
+#pragma unroll
+  for (int j = 0; j < kFirst; j++) ec[j] = k0 + j < k1 ? __ldg(&a.node_inc[k0 + j]) : -1;
+  TF x[kFirst][3];
+#pragma unroll
+  for (int j = 0; j < kFirst; j++)
+#pragma unroll
+    for (int i = 0; i < 3; i++) x[j][i] = ec[j] >= 0 ? __ldg(&fe[(long)(ec[j] >> 3) * 24 + (ec[j] & 7) * 3 + i]) : TF(0);
+#pragma unroll
+  for (int j = 0; j < kFirst; j++)
+    if (ec[j] >= 0) {
+#pragma unroll
+      for (int i = 0; i < 3; i++) fs[i] = kExact ? TF(__dadd_rn(double(fs[i]), double(x[j][i]))) : fs[i] + x[j][i];
+    }
+  for (int k = k0 + kFirst; k < k1; k++) {
     const int  ec = __ldg(&a.node_inc[k]);
     const long e  = ec >> 3;
     const int  c  = ec & 7;
 #pragma unroll
     for (int i = 0; i < 3; i++) {
-      const TF x = __ldg(&fe[e * 24 + c * 3 + i]);
-      fs[i]      = kExact ? TF(__dadd_rn(double(fs[i]), double(x))) : fs[i] + x;
+      const TF xi = __ldg(&fe[e * 24 + c * 3 + i]);
+      fs[i]       = kExact ? TF(__dadd_rn(double(fs[i]), double(xi))) : fs[i] + xi;
     }
   }
 #pragma unroll
@@ -182,7 +200,7 @@ __global__ void __launch_bounds__(256) k_node_update(NodeArgs a)
       v[i]   = axpy<kExact>(s.half, acc[i], a.v[i * ld + n]);
       u[i]   = a.u[i * ld + n];
     }
-    if (s.is_output && slot >= 0) apply_bc(bc, s.delta, s.time, a.ex, n, u, v);
+    if (s.is_output && slot >= 0) apply_bc(bc, s.delta, a.bc_expr_val ? a.bc_expr_val + (long)slot * 3 : nullptr, u, v);
   } else {
 #pragma unroll
     for (int i = 0; i < 3; i++) {
@@ -197,10 +215,11 @@ __global__ void __launch_bounds__(256) k_node_update(NodeArgs a)
     const StepSched s = a.sched[(long)(*a.step_base + a.k_pre) * a.num_groups + group];
 #pragma unroll
     for (int i = 0; i < 3; i++) v[i] = axpy<kExact>(s.half, acc[i], v[i]);
-    if (slot >= 0) apply_bc(bc, s.delta, s.time, a.ex, n, u, v);
+    const double* ev = a.bc_expr_val ? a.bc_expr_val + ((long)a.num_bc_slots + slot) * 3 : nullptr;
+    if (slot >= 0) apply_bc(bc, s.delta, ev, u, v);
 #pragma unroll
     for (int i = 0; i < 3; i++) u[i] = axpy<kExact>(s.delta, v[i], u[i]);
-    if (slot >= 0) apply_bc(bc, s.delta, s.time, a.ex, n, u, v);
+    if (slot >= 0) apply_bc(bc, s.delta, ev, u, v);
   }
 #pragma unroll
   for (int i = 0; i < 3; i++) {
@@ -218,6 +237,30 @@ cudaError_t launch_node_update(const NodeArgs& a, cudaStream_t stream)
     k_node_update<float, false><<<grid_for(a.N - a.n_begin, 256), 256, 0, stream>>>(a);
   else
     k_node_update<double, true><<<grid_for(a.N - a.n_begin, 256), 256, 0, stream>>>(a);
+  return cudaGetLastError();
+}
+
+__global__ void k_bc_expr_values(NodeArgs a, const int* __restrict__ slot_node, BcExprTable ex, double* __restrict__ out)
+{
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= a.num_bc_slots) return;
+  const NodeBC bc    = a.bcs[s];
+  const int    n     = slot_node[s];
+  const int    group = a.node_group ? a.node_group[n] : 0;
+  for (int level = 0; level < 2; level++) {
+    const int k = level == 0 ? a.k_post : a.k_pre;
+    if (k < 0) continue;
+    const double t = a.sched[(long)(*a.step_base + k) * a.num_groups + group].time;
+    for (int c = 0; c < 3; c++)
+      if (bc.expr[c] >= 0) out[((long)level * a.num_bc_slots + s) * 3 + c] = eval_bc_expression(ex, bc.expr[c], n, t);
+  }
+}
+
+cudaError_t launch_bc_expr_values(const NodeArgs& a, const int* slot_node, const BcExprTable& ex, double* out,
+                                  cudaStream_t stream)
+{
+  if (a.num_bc_slots == 0) return cudaSuccess;
+  k_bc_expr_values<<<grid_for(a.num_bc_slots, 128), 128, 0, stream>>>(a, slot_node, ex, out);
   return cudaGetLastError();
 }
 
@@ -243,7 +286,11 @@ __global__ void k_apply_bc(int N, long ld_n, const int* __restrict__ bc_slot, co
     uu[i] = u[i * ld_n + n];
     vv[i] = v[i * ld_n + n];
   }
-  apply_bc(bcs[slot], delta, time, ex, n, uu, vv);
+  const NodeBC& bc = bcs[slot];
+  double        ev[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) ev[k] = bc.expr[k] >= 0 ? eval_bc_expression(ex, bc.expr[k], n, time) : 0.0;
+  apply_bc(bc, delta, ev, uu, vv);
 #pragma unroll
   for (int i = 0; i < 3; i++) v[i * ld_n + n] = vv[i];
 }

@@ -152,10 +152,19 @@ struct NodeArgs {
   const double*     closure;  // or null
   int               closure_first, num_exact;
   const int*        node_off; // [num_groups + 1] first node of each sample
-  BcExprTable       ex;       // boundary-condition expressions
+  // expression-driven boundary conditions: their values for this launch,
+  // [2][num_bc_slots][3] (level 0 at the step finished, 1 at the step
+  // started; launch_bc_expr_values), or null when no condition has one
+  const double*     bc_expr_val;
+  int               num_bc_slots;
 };
 
 cudaError_t launch_node_update(const NodeArgs& a, cudaStream_t stream);
+// The values a.bc_expr_val holds for the node launch of `a` (k_post, k_pre):
+// each kinematic slot's expressions at its node (slot_node) and at the
+// schedule's time of those steps.
+cudaError_t launch_bc_expr_values(const NodeArgs& a, const int* slot_node, const BcExprTable& ex,
+                                  double* out, cudaStream_t stream);
 cudaError_t launch_advance_base(int* step_base, int k, cudaStream_t stream);
 
 // Kinematic conditions alone (ApplyKinematicConditions with delta_t), and

@@ -99,6 +99,10 @@ struct nsm_model {
   std::vector<int>         expr_start{0};       // [programs + 1]
   nsm::ExprOp*             d_expr_code = nullptr;
   int*                     d_expr_start = nullptr;
+  int                      num_bc_slots = 0;          // nodes with a kinematic condition
+  int*                     d_bc_slot_node = nullptr;  // [num_bc_slots] their node ids
+  bool                     bc_has_expr = false;       // some kinematic condition is an expression
+  double*                  d_bc_expr_val = nullptr;   // [2][num_bc_slots][3] values per node launch
   int*                d_bc_slot = nullptr;
   NodeBC*             d_bcs = nullptr;
   int*                d_ibc_slot = nullptr;
@@ -145,7 +149,7 @@ void free_all(nsm_model* m)
                   m->d_uf,   m->d_fe,   m->d_status,   m->d_step_base, m->d_scratch, m->d_stage,  m->d_out,   m->d_bc_slot,
                   m->d_bcs,  m->d_ibc_slot, m->d_ibcs,     m->d_sched, m->d_group_out, m->d_elem_group,
                   m->d_node_group, m->d_elem_off, m->d_mats, m->d_fallbacks, m->d_node_off, m->d_closure,
-                  m->d_stage_out, m->d_expr_code, m->d_expr_start};
+                  m->d_stage_out, m->d_expr_code, m->d_expr_start, m->d_bc_slot_node, m->d_bc_expr_val};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (cudaStream_t s : m->hp_stream)
@@ -183,12 +187,15 @@ int upload_bcs(nsm_model* m)
   for (int pass = 0; pass < 2; pass++) {
     std::vector<int>    slot(m->N, -1);
     std::vector<NodeBC> table;
+    std::vector<int>    slot_node;
+    bool                any_expr = false;
     for (const BcLine& b : m->bcs) {
       bool initial = b.kind == NSM_BC_INITIAL_VELOCITY;
       if ((pass == 0) == initial) continue;  // pass 0: kinematic lines, pass 1: initial velocity
       for (int n : b.nodes) {
         if (slot[n] < 0) {
           slot[n] = (int)table.size();
+          slot_node.push_back(n);
           NodeBC z;
           std::memset(&z, 0, sizeof(z));
           z.expr[0] = z.expr[1] = z.expr[2] = -1;
@@ -198,6 +205,7 @@ int upload_bcs(nsm_model* m)
         t.kind[b.component]  = (int8_t)(initial ? 1 : (b.kind == NSM_BC_PRESCRIBED_VELOCITY ? 1 : 2));
         t.value[b.component] = b.value;
         t.expr[b.component]  = (int8_t)b.expr;
+        any_expr             = any_expr || b.expr >= 0;
       }
     }
     int*&    d_slot = pass == 0 ? m->d_bc_slot : m->d_ibc_slot;
@@ -212,6 +220,21 @@ int upload_bcs(nsm_model* m)
     }
     if (m->N > 0)
       NSM_CUDA(cudaMemcpyAsync(d_slot, slot.data(), sizeof(int) * m->N, cudaMemcpyHostToDevice, m->stream));
+    if (pass == 0) {  // kinematic conditions: the node of each slot, value space for expressions
+      if (m->d_bc_slot_node) cudaFree(m->d_bc_slot_node);
+      if (m->d_bc_expr_val) cudaFree(m->d_bc_expr_val);
+      m->d_bc_slot_node = nullptr;
+      m->d_bc_expr_val  = nullptr;
+      m->num_bc_slots   = (int)table.size();
+      m->bc_has_expr    = any_expr;
+      if (any_expr) {
+        NSM_CUDA(cudaMalloc(&m->d_bc_slot_node, sizeof(int) * slot_node.size()));
+        NSM_CUDA(cudaMemcpyAsync(m->d_bc_slot_node, slot_node.data(), sizeof(int) * slot_node.size(),
+                                 cudaMemcpyHostToDevice, m->stream));
+        NSM_CUDA(cudaMalloc(&m->d_bc_expr_val, sizeof(double) * 6 * slot_node.size()));
+        NSM_CUDA(cudaMemsetAsync(m->d_bc_expr_val, 0, sizeof(double) * 6 * slot_node.size(), m->stream));
+      }
+    }
     NSM_CUDA(cudaStreamSynchronize(m->stream));  // host vectors go out of scope
   }
   // expression programs
@@ -311,7 +334,8 @@ nsm::NodeArgs node_args(nsm_model* m, int k_post, int k_pre, int gather_only)
   a.closure_first = m->closure_first;
   a.num_exact     = m->num_exact;
   a.node_off      = m->d_node_off;
-  a.ex            = expr_table(m);
+  a.bc_expr_val   = m->bc_has_expr ? m->d_bc_expr_val : nullptr;
+  a.num_bc_slots  = m->num_bc_slots;
   return a;
 }
 
@@ -347,12 +371,24 @@ std::pair<cudaEvent_t, cudaEvent_t> next_events(std::vector<std::pair<cudaEvent_
   return pool[used++];
 }
 
+// One node launch of the time loop, after the values of its expression
+// conditions when there are any.
+cudaError_t node_step(nsm_model* m, int k_post, int k_pre)
+{
+  const nsm::NodeArgs a = node_args(m, k_post, k_pre, 0);
+  if (m->bc_has_expr) {
+    cudaError_t e = nsm::launch_bc_expr_values(a, m->d_bc_slot_node, expr_table(m), m->d_bc_expr_val, m->stream);
+    if (e != cudaSuccess) return e;
+  }
+  return nsm::launch_node_update(a, m->stream);
+}
+
 // Launch sequence of a chunk of K schedule steps starting at the device base:
 // node(pre 0); {element(k); node(post k, pre k+1)}; node(post K-1); base += K.
 cudaError_t enqueue_chunk(nsm_model* m, int K, bool timed)
 {
   cudaError_t e;
-  if ((e = nsm::launch_node_update(node_args(m, -1, 0, 0), m->stream)) != cudaSuccess) return e;
+  if ((e = node_step(m, -1, 0)) != cudaSuccess) return e;
   for (int k = 0; k < K; k++) {
     if (timed) {
       auto ev = next_events(m->ev_elem, m->ev_elem_used);
@@ -361,13 +397,11 @@ cudaError_t enqueue_chunk(nsm_model* m, int K, bool timed)
       cudaEventRecord(ev.second, m->stream);
       auto en = next_events(m->ev_node, m->ev_node_used);
       cudaEventRecord(en.first, m->stream);
-      if ((e = nsm::launch_node_update(node_args(m, k, k + 1 < K ? k + 1 : -1, 0), m->stream)) != cudaSuccess)
-        return e;
+      if ((e = node_step(m, k, k + 1 < K ? k + 1 : -1)) != cudaSuccess) return e;
       cudaEventRecord(en.second, m->stream);
     } else {
       if ((e = launch_element(m, k)) != cudaSuccess) return e;
-      if ((e = nsm::launch_node_update(node_args(m, k, k + 1 < K ? k + 1 : -1, 0), m->stream)) != cudaSuccess)
-        return e;
+      if ((e = node_step(m, k, k + 1 < K ? k + 1 : -1)) != cudaSuccess) return e;
     }
   }
   return nsm::launch_advance_base(m->d_step_base, K, m->stream);

@@ -641,9 +641,9 @@ int create_impl(int S, const nsm_mesh_desc* meshes, int num_mats, const nsm_mate
     s.mass       = m->d_mass;
     s.inv_mass   = m->d_inv_mass;
     s.status     = m->d_status;
-    cudaError_t e = (E > 0) ? nsm::launch_setup(s, m->stream) : cudaSuccess;
+    cudaError_t e = nsm::launch_setup(s, m->stream);  // also for no elements: mass 0, the largest step
     m->dt_group.assign(S, 1.7976931348623157e308);
-    if (e == cudaSuccess && E > 0)
+    if (e == cudaSuccess)
       e = cudaMemcpyAsync(m->dt_group.data(), m->d_group_out, sizeof(double) * S, cudaMemcpyDeviceToHost, m->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(m->stream);  // host vectors live until here
     cudaFree(me);

@@ -277,13 +277,18 @@ cudaError_t launch_derived_element(int E, long ld_e, const int* conn, const doub
 
 cudaError_t launch_setup(const SetupArgs& a, cudaStream_t stream)
 {
-  k_setup_elements<<<grid_for(a.E, 128), 128, 0, stream>>>(a.E, a.ld_e, a.conn, a.X, a.ld_n, a.elem_group, a.mats,
-                                                           a.geo, a.me, a.dt_elem, a.status);
-  k_gather_mass<<<grid_for(a.N, 256), 256, 0, stream>>>(a.N, a.node_ptr, a.node_inc, a.me, a.ld_e, a.mass,
-                                                        a.inv_mass);
+  // (an empty mesh launches only the reductions, whose minimum over no
+  // element is the largest double)
+  if (a.E > 0)
+    k_setup_elements<<<grid_for(a.E, 128), 128, 0, stream>>>(a.E, a.ld_e, a.conn, a.X, a.ld_n, a.elem_group, a.mats,
+                                                             a.geo, a.me, a.dt_elem, a.status);
+  if (a.N > 0)
+    k_gather_mass<<<grid_for(a.N, 256), 256, 0, stream>>>(a.N, a.node_ptr, a.node_inc, a.me, a.ld_e, a.mass,
+                                                          a.inv_mass);
   if (a.num_groups == 1) {
     int blocks = grid_for(a.E, 256);
     if (blocks > 1024) blocks = 1024;
+    if (blocks < 1) blocks = 1;
     k_min_reduce<<<blocks, 256, 0, stream>>>(a.E, a.dt_elem, a.dt_partial);
     k_min_reduce<<<1, 256, 0, stream>>>(blocks, a.dt_partial, a.dt_out);
   } else {

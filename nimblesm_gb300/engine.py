@@ -549,9 +549,14 @@ def _concatenate(problems):
     no = np.cumsum([0] + [p.num_nodes for p in problems])
     coords = np.concatenate([p.coords for p in problems])
     conn = np.concatenate([p.conn + no[g] for g, p in enumerate(problems)]).astype(np.int32)
+    # the initial velocity fields, for all samples or none (a sample without
+    # nodes has none to give)
+    given = [p.v_init is not None for p in problems if p.num_nodes > 0]
+    if any(given) and not all(given):
+        raise ValueError("v_init must be given for every sample of an ensemble or for none")
     v0 = None
-    if all(p.v_init is not None for p in problems):
-        v0 = np.concatenate([p.v_init for p in problems])
+    if given and all(given):
+        v0 = np.concatenate([p.v_init if p.num_nodes > 0 else np.zeros((0, 3)) for p in problems])
     return Problem(coords=coords, conn=conn, node_sets={}, density=problems[0].density,
                    bulk_modulus=problems[0].bulk_modulus, shear_modulus=problems[0].shear_modulus, bcs=[],
                    v_init=v0)

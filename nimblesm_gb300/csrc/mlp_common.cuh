@@ -52,12 +52,13 @@ struct Scales {
   float min_det;    // det F bound of the training envelope
 };
 
-// GELU in its tanh form, 0.5 z (1 + tanh(c (z + 0.044715 z^3))),
-// c = sqrt(2/pi) (Hendrycks & Gimpel 2016), on the hardware tanh
-// (tanh.approx.f32, relative error about 2^-11, below the BF16 rounding of
-// the activations it produces).  Training, inference and the CPU oracle all
-// use this form.
-constexpr float kGeluC = 0.7978845608028654f, kGeluCB = 0.7978845608028654f * 0.044715f;
+// The activation: GELU in its sigmoid form, x sigma(1.702 x) (Hendrycks &
+// Gimpel 2016), written as a(u) = u (1 + tanh u) = 2 u sigma(2 u) with
+// u = 0.851 x.  The factors 0.851 and 1 / 1.702 sit in the adjacent layers'
+// weights, which training learns directly, so a pair of activations costs one
+// packed fused multiply-add and two hardware tanh (tanh.approx.f32, relative
+// error about 2^-11, below the BF16 rounding of the activations).  Training,
+// inference and the CPU oracle all use this form.
 
 __device__ __forceinline__ float tanh_approx(float u)
 {
@@ -65,18 +66,16 @@ __device__ __forceinline__ float tanh_approx(float u)
   asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(u));
   return t;
 }
-__device__ __forceinline__ float gelu(float z)
+__device__ __forceinline__ float act(float u)
 {
-  const float t  = tanh_approx(z * fmaf(kGeluCB, z * z, kGeluC));
-  const float hz = 0.5f * z;
-  return fmaf(hz, t, hz);
+  const float t = tanh_approx(u);
+  return fmaf(u, t, u);
 }
-__device__ __forceinline__ float gelu_grad(float z)
+// a'(u) = 1 + t + u (1 - t^2), t = tanh u
+__device__ __forceinline__ float act_grad(float u)
 {
-  const float z2 = z * z;
-  const float t  = tanh_approx(z * fmaf(kGeluCB, z2, kGeluC));
-  const float du = fmaf(3.0f * kGeluCB, z2, kGeluC);
-  return 0.5f * (1.0f + t) + 0.5f * z * (1.0f - t * t) * du;
+  const float t = tanh_approx(u);
+  return fmaf(u, fmaf(-t, t, 1.0f), 1.0f + t);
 }
 
 // ---- packed FP32x2 arithmetic (add/mul/fma .rn.f32x2, sm_100 and later) ----
@@ -109,19 +108,14 @@ __device__ __forceinline__ f32x2 f2_fma(f32x2 a, f32x2 b, f32x2 c)
   return d;
 }
 
-// Twice the GELU of two pre-activations, z + z tanh(u), packed to a BF16
-// pair (low half = first value).  Scaling by 2 commutes with every rounding
-// here, so this is exactly 2 * gelu() of each lane, and a next layer whose
-// weights are halved (also exact in BF16) computes bitwise what the
-// unscaled network computes, with one multiply per pair fewer.
-__device__ __forceinline__ uint32_t gelu_twice_bf16(f32x2 z)
+// The activation of two pre-activations, u + u tanh(u), packed to a BF16 pair
+// (low half = first value); each lane is bitwise act().
+__device__ __forceinline__ uint32_t act_bf16(f32x2 u)
 {
-  const f32x2 z2 = f2_mul(z, z);
-  const f32x2 in = f2_fma(f2_pack(kGeluCB, kGeluCB), z2, f2_pack(kGeluC, kGeluC));
-  float       u0, u1;
-  f2_unpack(f2_mul(z, in), u0, u1);
+  float u0, u1;
+  f2_unpack(u, u0, u1);
   float g0, g1;
-  f2_unpack(f2_fma(z, f2_pack(tanh_approx(u0), tanh_approx(u1)), z), g0, g1);
+  f2_unpack(f2_fma(u, f2_pack(tanh_approx(u0), tanh_approx(u1)), u), g0, g1);
   __nv_bfloat162 b = __floats2bfloat162_rn(g0, g1);
   return *reinterpret_cast<uint32_t*>(&b);
 }

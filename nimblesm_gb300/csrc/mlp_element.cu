@@ -73,8 +73,8 @@ __device__ __forceinline__ void layer(uint32_t d, const uint8_t* a, int Ka, cons
 }
 
 // Hidden-layer epilogue: 64 accumulator columns of this thread's row ->
-// 2 GELU(z + bias) -> BF16 row r of the [128][64] activation tile, two
-// columns per packed FP32x2 operation (the next layer's weights are halved).
+// act(z + bias) -> BF16 row r of the [128][64] activation tile, two columns
+// per packed FP32x2 operation.
 __device__ __forceinline__ void hidden_epilogue(uint32_t taddr, const float* bias, uint8_t* tile, int r)
 {
 #pragma unroll
@@ -89,7 +89,7 @@ __device__ __forceinline__ void hidden_epilogue(uint32_t taddr, const float* bia
       for (int j = 0; j < 4; j++) {
         f32x2 v = f2_pack(z[k0 + 2 * j], z[k0 + 2 * j + 1]);
         if (bias) v = f2_add(v, *reinterpret_cast<const f32x2*>(bias + 16 * h + k0 + 2 * j));
-        w[j] = gelu_twice_bf16(v);
+        w[j] = act_bf16(v);
       }
       *reinterpret_cast<uint4*>(tile + kmajor_offset(r, 16 * h + k0, kHid)) = make_uint4(w[0], w[1], w[2], w[3]);
     }
@@ -153,21 +153,9 @@ __global__ void __launch_bounds__(128) k_element_mlp(ElementArgs a, MlpElementAr
     err = 0;
   }
   {
-    // W1x as is; W2 and W3x halved (exact in BF16), for the doubled activations
+    // the layers' BF16 weight images
     const uint4* src = reinterpret_cast<const uint4*>(m.img);
-    for (int i = r; i < kOffW2t / 16; i += 128) {
-      uint4 v = src[i];
-      if (i >= kOffW2 / 16) {
-        const __nv_bfloat162 half2 = __floats2bfloat162_rn(0.5f, 0.5f);
-        uint32_t*            q     = reinterpret_cast<uint32_t*>(&v);
-#pragma unroll
-        for (int j = 0; j < 4; j++) {
-          __nv_bfloat162 h = __hmul2(*reinterpret_cast<__nv_bfloat162*>(&q[j]), half2);
-          q[j]             = *reinterpret_cast<uint32_t*>(&h);
-        }
-      }
-      reinterpret_cast<uint4*>(sm + el::W)[i] = v;
-    }
+    for (int i = r; i < kOffW2t / 16; i += 128) reinterpret_cast<uint4*>(sm + el::W)[i] = src[i];
     float* bias = reinterpret_cast<float*>(sm + el::B);
     if (r < kHid) bias[r] = m.P[ob2 + r];
     if (r < kOut) bias[64 + r] = m.P[ob3 + r];

@@ -255,7 +255,7 @@ __global__ void __launch_bounds__(128) k_train(const float* __restrict__ X, cons
   {
     float z[64];
     ld_row(tb, tr::cZ1, 4, z);
-    for (int q = 0; q < 64; q++) z[q] = gelu(z[q]);
+    for (int q = 0; q < 64; q++) z[q] = act(z[q]);
     for (int k0 = 0; k0 < 64; k0 += 8) store_chunk(sm + tr::A1, r, k0, kHid, z + k0);
     for (int q = 0; q < 64; q++) store_bf16(sm + tr::BOP, q, r, 128, z[q]);
   }
@@ -268,7 +268,7 @@ __global__ void __launch_bounds__(128) k_train(const float* __restrict__ X, cons
   {
     float z[64];
     ld_row(tb, tr::cZ2, 4, z);
-    for (int q = 0; q < 64; q++) z[q] = gelu(z[q] + b2[q]);
+    for (int q = 0; q < 64; q++) z[q] = act(z[q] + b2[q]);
     for (int k0 = 0; k0 < 64; k0 += 8) store_chunk(sm + tr::A2, r, k0, kHid, z + k0);
     for (int q = 0; q < 64; q++) store_bf16(sm + tr::BOP3, q, r, 128, z[q]);
   }
@@ -303,7 +303,7 @@ __global__ void __launch_bounds__(128) k_train(const float* __restrict__ X, cons
     float da[64], z[64];
     ld_row(tb, tr::cDA2, 4, da);
     ld_row(tb, tr::cZ2, 4, z);
-    for (int q = 0; q < 64; q++) da[q] *= gelu_grad(z[q] + b2[q]);
+    for (int q = 0; q < 64; q++) da[q] *= act_grad(z[q] + b2[q]);
     for (int k0 = 0; k0 < 64; k0 += 8) store_chunk(sm + tr::DZ2, r, k0, kHid, da + k0);
     for (int q = 0; q < 64; q++) store_bf16(sm + tr::AOP, q, r, 128, da[q]);
   }
@@ -317,7 +317,7 @@ __global__ void __launch_bounds__(128) k_train(const float* __restrict__ X, cons
     float da[64], z[64];
     ld_row(tb, tr::cDA1, 4, da);
     ld_row(tb, tr::cZ1, 4, z);
-    for (int q = 0; q < 64; q++) store_bf16(sm + tr::AOP, 64 + q, r, 128, da[q] * gelu_grad(z[q]));
+    for (int q = 0; q < 64; q++) store_bf16(sm + tr::AOP, 64 + q, r, 128, da[q] * act_grad(z[q]));
   }
   publish_operands();
   // weight gradients: sums over the 128 points of the tile (K = points)
@@ -451,7 +451,7 @@ __global__ void __launch_bounds__(128) k_predict(long n, const float* __restrict
   {
     float z[64];
     ld_row(tb, inf::cZ1, 4, z);
-    for (int q = 0; q < 64; q++) z[q] = gelu(z[q]);
+    for (int q = 0; q < 64; q++) z[q] = act(z[q]);
     for (int k0 = 0; k0 < 64; k0 += 8) store_chunk(sm + inf::A1, r, k0, kHid, z + k0);
   }
   publish_operands();
@@ -463,7 +463,7 @@ __global__ void __launch_bounds__(128) k_predict(long n, const float* __restrict
   {
     float z[64];
     ld_row(tb, inf::cZ2, 4, z);
-    for (int q = 0; q < 64; q++) z[q] = gelu(z[q] + b2[q]);
+    for (int q = 0; q < 64; q++) z[q] = act(z[q] + b2[q]);
     for (int k0 = 0; k0 < 64; k0 += 8) store_chunk(sm + inf::A2, r, k0, kHid, z + k0);
   }
   publish_operands();

@@ -1,7 +1,7 @@
 """CPU oracle of the learned closure's network (TEST INFRASTRUCTURE ONLY).
 
 The engine's MLP (nimblesm_gb300/csrc/mlp_common.cuh): sigma/G = L(H) +
-s_r * |x|^2 * MLP(x), x = H * s_in, MLP = 9 -> 64 -> 64 -> 6 with GELU (tanh
+s_r * |x|^2 * MLP(x), x = H * s_in, MLP = 9 -> 64 -> 64 -> 6 with GELU (sigmoid
 form), evaluated with BF16 operands and FP32 accumulation on the tensor
 cores.  This module restates the
 forward pass and the gradient of the training loss in float64 numpy, either
@@ -39,17 +39,16 @@ def linear_part(H, k_over_g):
                      H[:, 1] + H[:, 3], H[:, 5] + H[:, 7], H[:, 6] + H[:, 2]], axis=1)
 
 
-GELU_C = np.sqrt(2.0 / np.pi)
+def act(u):
+    """The engine's activation: GELU in its sigmoid form x sigma(1.702 x)
+    (Hendrycks & Gimpel 2016), written a(u) = u (1 + tanh u) = 2 u sigma(2u)
+    with u = 0.851 x, the constant factors being the adjacent layers'."""
+    return u * (1.0 + np.tanh(u))
 
 
-def gelu(z):
-    """GELU, tanh form (the engine's activation)."""
-    return 0.5 * z * (1.0 + np.tanh(GELU_C * (z + 0.044715 * z ** 3)))
-
-
-def gelu_grad(z):
-    t = np.tanh(GELU_C * (z + 0.044715 * z ** 3))
-    return 0.5 * (1.0 + t) + 0.5 * z * (1.0 - t * t) * GELU_C * (1.0 + 3 * 0.044715 * z * z)
+def act_grad(u):
+    t = np.tanh(u)
+    return 1.0 + t + u * (1.0 - t * t)
 
 
 def forward(P, scales, H, emulate=True):
@@ -64,9 +63,9 @@ def forward(P, scales, H, emulate=True):
     W1x = np.zeros((HID, 32))
     W1x[:, :9], W1x[:, 9], W1x[:, 16:25] = W1, b1, W1
     z1 = X @ r(W1x).T
-    a1 = r(gelu(z1))
+    a1 = r(act(z1))
     z2 = a1 @ r(W2).T + b2
-    a2 = r(gelu(z2))
+    a2 = r(act(z2))
     out = a2 @ r(W3).T + b3
     return dict(X=X, z1=z1, a1=a1, z2=z2, a2=a2, out=out)
 
@@ -93,9 +92,9 @@ def loss_and_gradient(P, scales, H, Y, emulate=True):
     loss = float((d * d).sum() / n)
     g = r(2.0 * d / n)
     dW3, db3 = g.T @ f["a2"], g.sum(axis=0)
-    dz2 = r((g @ r(W3)) * gelu_grad(f["z2"]))
+    dz2 = r((g @ r(W3)) * act_grad(f["z2"]))
     dW2, db2 = dz2.T @ f["a1"], dz2.sum(axis=0)
-    dz1 = r((dz2 @ r(W2)) * gelu_grad(f["z1"]))
+    dz1 = r((dz2 @ r(W2)) * act_grad(f["z1"]))
     dW1x = dz1.T @ f["X"]
     grad = np.zeros(NPARAMS)
     grad[oW1:ob1] = (dW1x[:, :9] + dW1x[:, 16:25]).ravel()

@@ -47,7 +47,7 @@ FP64_FLOPS_PER_IP = 261.1
 FP64_INSTR_PER_IP = 173.2
 # DRAM bytes (read + write) of one element launch on the 128^3 cube, from one
 # ncu capture per form (profiles/k_element_traffic_cube128.md).
-ELEMENT_TRAFFIC_128 = {"fp64": 2.671848192e9 + 2.499607296e9, "fp32": 0.119998720e9 + 1.217577728e9}
+ELEMENT_TRAFFIC_128 = {"fp64": 2.671848192e9 + 2.499607296e9, "fp32": 0.119155456e9 + 1.213316608e9}
 
 
 def algorithmic_bytes(N, E, precision):
@@ -219,6 +219,42 @@ def uq_variants(E, args, device):
             "clocks": clk.summary()}
         m.close()
     return out
+
+
+def uq_closure_variant(E, args, problem, device):
+    """The reference's UQ mode on the 128^3 mesh in one handle: the nominal
+    trajectory, 2 exact samples (element forces with their own bulk and
+    shear moduli, +-5% of the nominal's) and 8 approximate samples whose force
+    is the linear closure c0 f_nominal + sum_k c_k f_exact_k.  One element
+    launch covers the nominal's and the exact samples' elements; the closure
+    is formed inside the node launch.  Sample values and closure coefficients
+    are synthetic (seeded).  value counts the element work (integration-point
+    updates of the nominal and exact trajectories)."""
+    from nimblesm_gb300.uq import UqSpec
+    rng = np.random.default_rng(5)
+    n_exact, n_approx = 2, 8
+    params = [(0, "bulk_modulus", 0.1 * problem.bulk_modulus), (0, "shear_modulus", 0.1 * problem.shear_modulus)]
+    exact = np.array([[-0.5, 0.5], [0.5, -0.5]])
+    approx = rng.uniform(-0.5, 0.5, (n_approx, 2))
+    w = rng.uniform(0.0, 0.5, (n_approx, n_exact))
+    coef = np.concatenate([1.0 - w.sum(axis=1, keepdims=True), w], axis=1)
+    spec = UqSpec(params, exact, approx, coef)
+    dt = 0.5 * critical_time_step(problem)
+    steps = args.uq_closure_steps
+    m = E.UqModel(problem, spec, device=device)
+    m.begin(SCHEDULE_STEPS * dt, SCHEDULE_STEPS, SCHEDULE_STEPS)
+    m.advance(3)
+    m.synchronize()
+    with ClockSampler(device) as clk:
+        ms = m.advance_timed(steps)
+    S = 1 + n_exact + n_approx
+    res = {"uq_closure": {
+        "value": 8.0 * problem.num_elem * (1 + n_exact) * steps / (ms * 1e-3), "unit": UNIT,
+        "ms_per_step": ms / steps, "trajectories": S, "exact_samples": n_exact, "approximate_samples": n_approx,
+        "trajectory_steps_per_s": S * steps / (ms * 1e-3), "elements_per_trajectory": problem.num_elem,
+        "steps_timed": steps, "after_steps": 3 + steps, "clocks": clk.summary()}}
+    m.close()
+    return res
 
 
 def big_fp32_variant(E, args, device):
@@ -453,6 +489,8 @@ def run_ours(args):
         variants.update(uq_variants(E, args, local))
     if args.variants and args.big_steps > 0:
         variants.update(big_fp32_variant(E, args, local))
+    if args.variants and args.uq_closure_steps > 0:
+        variants.update(uq_closure_variant(E, args, problem, local))
     mlp = None
     if args.variants and args.mlp_steps > 0:
         fp32_value = variants.get("fp32", {}).get("value", float("nan"))
@@ -487,6 +525,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--uq-steps", type=int, default=100, help="timed steps of the 512-sample ensemble (0: skip)")
     ap.add_argument("--uq-samples", type=int, default=512)
+    ap.add_argument("--uq-closure-steps", type=int, default=20,
+                    help="timed steps of the reference-style UQ mode on the main mesh (0: skip)")
     ap.add_argument("--big-n", type=int, default=256, help="cube divisions of the large FP32-mixed variant")
     ap.add_argument("--big-steps", type=int, default=20, help="timed steps of the large variant (0: skip)")
     ap.add_argument("--mlp-steps", type=int, default=103, help="steps of the learned-closure run (0: skip)")

@@ -134,7 +134,18 @@ __device__ __forceinline__ void point_gradient(const float x[8][3], const float 
   }
 }
 
-__global__ void __launch_bounds__(128) k_element_mlp(ElementArgs a, MlpElementArgs m)
+// A warp holds 4 consecutive elements x 8 points.  Its 32 point records
+// (plane p, elements e..e+3: 256 contiguous bytes per plane) go out through
+// the warp's 2 KB slice of the input tile, two planes per store instruction
+// (512 bytes in two 256-byte runs), instead of 16-byte pieces a record apart.
+// Slot swizzle: conflict-free for the per-lane writes (8 consecutive lanes,
+// one chunk) and for the reads (two lanes 8 apart, four chunks each).
+__device__ __forceinline__ int rec_slot(int row, int c)
+{
+  return ((row ^ ((row >> 3) & 1)) << 2) + (c ^ ((row >> 1) & 3));
+}
+
+__global__ void __launch_bounds__(128, 5) k_element_mlp(ElementArgs a, MlpElementArgs m)
 {
   extern __shared__ __align__(1024) uint8_t sm[];
   __shared__ uint64_t mbar;
@@ -300,18 +311,35 @@ __global__ void __launch_bounds__(128) k_element_mlp(ElementArgs a, MlpElementAr
     C[2][2] = F[0][0] * F[1][1] - F[0][1] * F[1][0];
     const float J = F[0][0] * C[0][0] + F[0][1] * C[0][1] + F[0][2] * C[0][2];
     if (valid && (!(J > 0.0f) || !(det0 > 0.0f))) status |= NSM_STATUS_BAD_JACOBIAN;
-    if (valid && store) {
-      float rr[kIpRecord];
+    if (store) {
+      const long e_first = chunk * el::kElems + 4 * warp;  // the warp's elements e_first .. e_first + 3
+      float      rr[kIpRecord];
 #pragma unroll
       for (int i = 0; i < 3; i++)
 #pragma unroll
         for (int k = 0; k < 3; k++) rr[full_slot(i, k)] = F[i][k];
 #pragma unroll
       for (int q = 0; q < 6; q++) rr[9 + q] = sig[q];
-      rr[15]     = 0.0f;
-      float* dst = reinterpret_cast<float*>(a.ip) + ((size_t)p * ld_e + e) * kIpRecord;
+      rr[15] = 0.0f;
+      if (e_first + 4 <= a.E) {
+        float4* tile = reinterpret_cast<float4*>(stage);  // free until the next chunk's staging
 #pragma unroll
-      for (int k = 0; k < kIpRecord; k += 4) *reinterpret_cast<float4*>(dst + k) = make_float4(rr[k], rr[k + 1], rr[k + 2], rr[k + 3]);
+        for (int c = 0; c < 4; c++)
+          tile[rec_slot(lane, c)] = make_float4(rr[4 * c], rr[4 * c + 1], rr[4 * c + 2], rr[4 * c + 3]);
+        __syncwarp();
+        float4* ip4 = reinterpret_cast<float4*>(a.ip);
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+          const int plane = 2 * k + (lane >> 4), j = lane & 15;  // chunk j of the plane's 4 records
+          ip4[((size_t)plane * ld_e + e_first) * 4 + j] = tile[rec_slot((j >> 2) * 8 + plane, j & 3)];
+        }
+        __syncwarp();  // the slice is read before the next chunk's staging
+      } else if (valid) {
+        float* dst = reinterpret_cast<float*>(a.ip) + ((size_t)p * ld_e + e) * kIpRecord;
+#pragma unroll
+        for (int k = 0; k < kIpRecord; k += 4)
+          *reinterpret_cast<float4*>(dst + k) = make_float4(rr[k], rr[k + 1], rr[k + 2], rr[k + 3]);
+      }
     }
     float S[3][3];  // S[d][i] = det0 sum_J G0[d][J] P[i][J],  P = sigma cof(F)
     {

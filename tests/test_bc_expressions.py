@@ -84,3 +84,57 @@ def test_expression_run_against_the_reference():
         assert rel(st["v"], fx["v"][t]) <= 1e-10, (t, rel(st["v"], fx["v"][t]))
     assert rel(st["F"], fx["F"]) <= 1e-10 and rel(st["sigma"], fx["sigma"]) <= 1e-10
     m.close()
+
+
+def _random_expression(rng, depth=0):
+    """A random expression of the reference's grammar: numbers (plain,
+    decimal, exponent forms), x y z t, e pi tau, + - * / % ^, unary minus,
+    parentheses, the math functions, and conditions under "? :"."""
+    leaves = ["x", "y", "z", "t", "e", "pi", "tau", "2", "0.5", "3.25", "1e-3", "2.5e2", "7"]
+    if depth > 3 or rng.random() < 0.25:
+        return str(rng.choice(leaves))
+    k = rng.integers(0, 10)
+    a = _random_expression(rng, depth + 1)
+    if k <= 4:
+        op = str(rng.choice(["+", "-", "*", "/", "%"]))
+        return f"{a} {op} {_random_expression(rng, depth + 1)}"
+    if k == 5:
+        return f"({a})"
+    if k == 6:
+        return f"-({a})"
+    if k == 7:
+        f = str(rng.choice(["sin", "cos", "exp", "abs", "atan", "sqrt", "floor", "ceil", "round", "cbrt", "erf"]))
+        return f"{f}({a})"
+    if k == 8:
+        return f"({a})^{rng.choice(['2', '3', '0.5', '-1'])}"
+    cmp = str(rng.choice([">", "<", ">=", "<="]))
+    return f"{a} {cmp} {_random_expression(rng, depth + 1)} ? {_random_expression(rng, depth + 1)} : {a}"
+
+
+def test_random_expressions_against_the_reference_parser():
+    """400 seeded random expressions at 3 points: the engine's host
+    evaluation equals the reference parser's value bit for bit (NaN for NaN),
+    or both refuse the text.  Needs the reference built from its sources
+    (oracle/_ref), so it runs where those sources are."""
+    from oracle import oracle as O
+    if not O.reference_available():
+        pytest.skip("the reference library is not built here")
+    rng = np.random.default_rng(2024)
+    pts = [(0.3, 0.7, 0.25, 1.0e-6), (0.75, 0.2, 0.5, 5.0e-6), (1.0, 0.0, 0.125, 0.0)]
+    checked = 0
+    for _ in range(400):
+        text = _random_expression(rng)
+        for pt in pts:
+            try:
+                ref = O.ref_eval_expression(text, *pt)
+            except ValueError:
+                ref = None
+            try:
+                ours = E.bc_expression_eval(text, *pt)
+            except E.EngineError:
+                ours = None
+            assert (ref is None) == (ours is None), (text, ref, ours)
+            if ref is not None:
+                assert ours == ref or (np.isnan(ours) and np.isnan(ref)), (text, pt, ours, ref)
+                checked += 1
+    assert checked > 900  # most of them parse

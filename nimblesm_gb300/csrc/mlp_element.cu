@@ -194,46 +194,47 @@ __global__ void __launch_bounds__(128, 5) k_element_mlp(ElementArgs a, MlpElemen
     const long e = c * el::kElems + el;
     return (c < nchunks && e < a.E) ? __ldg(&a.conn[p * ld_e + e]) : -1;
   };
-  auto values_of = [&](int id, float4& v0, float4& v1) {
-    if (id >= 0) {
-      v0 = make_float4(__ldg(&a.uf[id]), __ldg(&a.uf[ld_n + id]), __ldg(&a.uf[2 * ld_n + id]), __ldg(&a.Xf[id]));
-      v1 = make_float4(__ldg(&a.Xf[ld_n + id]), __ldg(&a.Xf[2 * ld_n + id]), 0.0f, 0.0f);
-    } else {  // idle rows: zero displacement on a unit cube
-      v0 = make_float4(0.0f, 0.0f, 0.0f, (float)sx_of(p));
-      v1 = make_float4((float)sy_of(p), (float)sz_of(p), 0.0f, 0.0f);
-    }
+  auto values_of = [&](int id, float4& v) {
+    v = id >= 0 ? make_float4(__ldg(&a.uf[id]), __ldg(&a.uf[ld_n + id]), __ldg(&a.uf[2 * ld_n + id]), 0.0f)
+                : make_float4(0.0f, 0.0f, 0.0f, 0.0f);  // idle rows: zero displacement
   };
   int    id_next = node_of(blockIdx.x);
-  float4 nv0, nv1;
-  values_of(id_next, nv0, nv1);
+  float4 nv;
+  values_of(id_next, nv);
   for (long chunk = blockIdx.x; chunk < nchunks; chunk += gridDim.x) {
     const long e     = chunk * el::kElems + el;
     const bool valid = e < a.E;
 
-    // ---- gather: node p of the element, staged for the element's 8 lanes ----
-    {
-      float4* st = reinterpret_cast<float4*>(stage + (lane >> 3) * 256 + p * 32);
-      st[0]      = nv0;
-      st[1]      = nv1;
+    // ---- the point's reference geometry (computed when the closure was attached) ----
+    float G0[3][3], det0, h[9];
+    if (valid) {
+      const float4* gp = reinterpret_cast<const float4*>(m.geo + ((size_t)e * 8 + p) * 12);
+      const float4  g0 = __ldg(gp), g1 = __ldg(gp + 1), g2 = __ldg(gp + 2);
+      G0[0][0] = g0.x, G0[0][1] = g0.y, G0[0][2] = g0.z, G0[1][0] = g0.w;
+      G0[1][1] = g1.x, G0[1][2] = g1.y, G0[2][0] = g1.z, G0[2][1] = g1.w;
+      G0[2][2] = g2.x, det0 = g2.y;
+    } else {  // idle rows: a unit element
+#pragma unroll
+      for (int q = 0; q < 9; q++) G0[q / 3][q % 3] = q % 4 == 0 ? 1.0f : 0.0f;
+      det0 = 1.0f;
     }
+
+    // ---- gather: node p's displacement, staged for the element's 8 lanes ----
+    reinterpret_cast<float4*>(stage + (lane >> 3) * 128)[p] = nv;
     __syncwarp();
-    float Du[3][3], DX[3][3];
+    float Du[3][3];
     {
-      float         xu[8][3], xX[8][3];
-      const float4* st = reinterpret_cast<const float4*>(stage + (lane >> 3) * 256);
+      float         xu[8][3];
+      const float4* st = reinterpret_cast<const float4*>(stage + (lane >> 3) * 128);
 #pragma unroll
       for (int n = 0; n < 8; n++) {
-        const float4 v0 = st[2 * n], v1 = st[2 * n + 1];
-        xu[n][0] = v0.x, xu[n][1] = v0.y, xu[n][2] = v0.z;
-        xX[n][0] = v0.w, xX[n][1] = v1.x, xX[n][2] = v1.y;
+        const float4 v = st[n];
+        xu[n][0] = v.x, xu[n][1] = v.y, xu[n][2] = v.z;
       }
       point_gradient(xu, w, Du);
-      point_gradient(xX, w, DX);
     }
     __syncwarp();  // the staging area is overwritten by this warp's input rows below
 
-    float G0[3][3], det0, h[9];
-    invert3<float>(DX, G0, det0);
 #pragma unroll
     for (int i = 0; i < 3; i++)
 #pragma unroll
@@ -262,7 +263,7 @@ __global__ void __launch_bounds__(128, 5) k_element_mlp(ElementArgs a, MlpElemen
       layer(tb, sm + el::A, kHid, sm + el::W + kOffW2, kHid);
       mma_commit(&mbar);
     }
-    values_of(id_next, nv0, nv1);
+    values_of(id_next, nv);
     wait_commit(&mbar, phase, &err);
     hidden_epilogue(taddr, b2, sm + el::A, r);
     // ---- layer 3 ----
@@ -408,6 +409,39 @@ __global__ void __launch_bounds__(128, 5) k_element_mlp(ElementArgs a, MlpElemen
   }
   __syncthreads();
   if (warp == 0) tmem_dealloc(tb, el::kCols);
+}
+
+// Reference geometry of every point for the closure kernel: the same
+// gather, point gradient and inverse the kernel formed per step before.
+__global__ void k_closure_geometry(ElementArgs a, float* __restrict__ geo)
+{
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= 8L * a.E) return;
+  const long e = i >> 3;
+  const int  p = (int)(i & 7);
+  float      w[3][2][2];
+  point_weights(p, w);
+  float x[8][3];
+#pragma unroll
+  for (int n = 0; n < 8; n++) {
+    const int id = __ldg(&a.conn[n * a.ld_e + e]);
+#pragma unroll
+    for (int k = 0; k < 3; k++) x[n][k] = __ldg(&a.Xf[k * a.ld_n + id]);
+  }
+  float DX[3][3], G0[3][3], det0;
+  point_gradient(x, w, DX);
+  invert3<float>(DX, G0, det0);
+  float4* out = reinterpret_cast<float4*>(geo + i * 12);
+  out[0]      = make_float4(G0[0][0], G0[0][1], G0[0][2], G0[1][0]);
+  out[1]      = make_float4(G0[1][1], G0[1][2], G0[2][0], G0[2][1]);
+  out[2]      = make_float4(G0[2][2], det0, 0.0f, 0.0f);
+}
+
+cudaError_t launch_closure_geometry(const ElementArgs& a, float* geo, cudaStream_t stream)
+{
+  if (a.E == 0) return cudaSuccess;
+  k_closure_geometry<<<(unsigned)((8L * a.E + 127) / 128), 128, 0, stream>>>(a, geo);
+  return cudaGetLastError();
 }
 
 static int g_blocks_per_sm = 0;

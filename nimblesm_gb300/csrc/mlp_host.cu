@@ -93,6 +93,7 @@ bool element_args(nsm_mlp* m, MlpElementArgs* out, double* bulk, double* shear)
   out->img = m->d_img;
   out->P   = m->d_P;
   out->sc  = m->sc;
+  out->geo = nullptr;  // the model's (nsm_set_mlp_closure)
   if (bulk) *bulk = m->K;
   if (shear) *shear = m->G;
   return true;

@@ -91,6 +91,7 @@ struct nsm_model {
   std::vector<double> dt_group;    // per-sample critical time step
   nsm::ElementLaunch  elaunch{128, 0, 0, 0};
   nsm_mlp*            closure = nullptr;        // learned material (FP32 form), or null
+  float*              d_closure_geo = nullptr;  // [ld_e][8][12] its reference geometry per point
   unsigned long long* d_fallbacks = nullptr;    // points that left the closure's envelope
 
   std::vector<BcLine> bcs;
@@ -149,7 +150,8 @@ void free_all(nsm_model* m)
                   m->d_uf,   m->d_fe,   m->d_status,   m->d_step_base, m->d_scratch, m->d_stage,  m->d_out,   m->d_bc_slot,
                   m->d_bcs,  m->d_ibc_slot, m->d_ibcs,     m->d_sched, m->d_group_out, m->d_elem_group,
                   m->d_node_group, m->d_elem_off, m->d_mats, m->d_fallbacks, m->d_node_off, m->d_closure,
-                  m->d_stage_out, m->d_expr_code, m->d_expr_start, m->d_bc_slot_node, m->d_bc_expr_val};
+                  m->d_stage_out, m->d_expr_code, m->d_expr_start, m->d_bc_slot_node, m->d_bc_expr_val,
+                  m->d_closure_geo};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (cudaStream_t s : m->hp_stream)
@@ -354,6 +356,7 @@ cudaError_t launch_element(nsm_model* m, int k)
     nsm::mlp::MlpElementArgs ma;
     nsm::mlp::element_args(m->closure, &ma, nullptr, nullptr);
     ma.fallback_count = m->d_fallbacks;
+    ma.geo            = m->d_closure_geo;
     return nsm::mlp::launch_element_mlp(a, ma, m->stream);
   }
   return m->precision == NSM_PRECISION_FP64 ? nsm::launch_element_fp64(a, m->elaunch, m->stream)
@@ -1380,6 +1383,10 @@ int nsm_set_mlp_closure(nsm_model* m, nsm_mlp* closure)
   if (!m->d_fallbacks) {
     NSM_CUDA(cudaMalloc(&m->d_fallbacks, sizeof(unsigned long long)));
     NSM_CUDA(cudaMemsetAsync(m->d_fallbacks, 0, sizeof(unsigned long long), m->stream));
+  }
+  if (closure && !m->d_closure_geo) {  // the reference geometry of every point, once
+    NSM_CUDA(cudaMalloc(&m->d_closure_geo, sizeof(float) * 96 * (size_t)m->ld_e));
+    NSM_CUDA(nsm::mlp::launch_closure_geometry(element_args(m, -1), m->d_closure_geo, m->stream));
   }
   m->closure = closure;
   for (auto& g : m->graphs) cudaGraphExecDestroy(g.second);

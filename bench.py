@@ -99,6 +99,15 @@ class ClockSampler:
                 self.proc.wait(timeout=5)
             except Exception:
                 self.proc.kill()
+            # a region shorter than the sampler's start-up: one sample at its end
+            try:
+                if not open(self.path).read().strip():
+                    with open(self.path, "w") as f:
+                        subprocess.run(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                        "--format=csv,noheader,nounits"], stdout=f, stderr=subprocess.DEVNULL,
+                                       timeout=10)
+            except Exception:
+                pass
 
     def summary(self):
         try:

@@ -219,6 +219,46 @@ int nsm_host_chunks(nsm_model* model, int* chunks);
  * F: [E][8][9], sigma: [E][8][6]; either may be NULL. */
 int nsm_get_ip_data(nsm_model* model, double* F, double* sigma);
 
+/* ---- block materials computed outside the engine (the plugin path) ----
+ * The reference's BlockMaterialInterface (src/nimble_block_material_interface_base.h:52-84,
+ * created by BlockMaterialInterfaceFactoryBase::create,
+ * src/nimble_block_material_interface_factory_base.h:59-72) computes the stress of whole blocks on
+ * the device between the kinematics and the stress divergence
+ * (src/nimble_kokkos_model_data.cc:1180-1286), from F and sigma at steps n and n+1 and the
+ * per-point state (Material::GetStress's device form, src/nimble_material.h:255-287).  With a
+ * callback registered for a block, each step of the model runs the same split: the engine writes
+ * F at n+1 of every point (and the built-in blocks' sigma), calls the callback of each such block
+ * with device views of its points, then forms the nodal forces from the recorded sigma.  The
+ * callback enqueues its own kernels on `stream` and returns 0 (nonzero: the step fails with
+ * NSM_ERR_STATE); it must not synchronise the stream.  Record and state buffers of steps n and n+1
+ * alternate after every step, as UpdateStates swaps the reference's element data.  A model with a
+ * callback steps without CUDA graphs, so that the callback sees every step's times. */
+typedef struct nsm_stress_request {
+  int         block;                    /* block index, 0-based in the model's block order */
+  int         elem_begin, elem_end;     /* the block's elements [begin, end) (blocks are contiguous) */
+  int         precision;                /* NSM_PRECISION_FP64: double records, FP32_MIXED: float records */
+  long        ld_e;                     /* record plane stride */
+  const void* records_n;                /* step n:   [8 points][ld_e][16], F in slots 0..8 (K_F order), sigma 9..14 (K_S) */
+  void*       records_np1;              /* step n+1: F written by the engine; the callback writes slots 9..14 */
+  int         num_state;                /* state variables per point (as registered) */
+  const double* state_n;                /* [8][ld_e][num_state] at step n, or NULL */
+  double*       state_np1;              /* the same at n+1, written by the callback */
+  double      time_n, time_np1;
+  double      density, bulk_modulus, shear_modulus;  /* the block's material parameters */
+  void*       stream;                   /* cudaStream_t */
+} nsm_stress_request;
+typedef int (*nsm_stress_callback)(void* user, const nsm_stress_request* request);
+/* Registers `fn` for block `block` (replacing its built-in material) with num_state variables per
+ * point (0 .. 64); NULL removes it.  Single-mesh models only (not ensembles or the UQ mode). */
+int nsm_set_block_material_callback(nsm_model* model, int block, int num_state, nsm_stress_callback fn, void* user);
+/* The per-point state after the last step, [E][8][num_state] (the largest registered count). */
+int nsm_get_state_data(nsm_model* model, double* state);
+/* Two callbacks written with the engine's own arithmetic, e.g. to check the path: the neo-Hookean
+ * stress from F at n+1 (stateless), and the same with one history variable per point,
+ * state_np1 = state_n + |det F_np1 - det F_n|. */
+int nsm_example_neohookean_callback(void* user, const nsm_stress_request* request);
+int nsm_example_history_callback(void* user, const nsm_stress_request* request);
+
 /* Derived element output of the current configuration (replaces
  * Block::ComputeDerivedElementData, src/nimble_block.cc:438-497, through
  * HexElement::ComputeVolumeAverage, src/nimble_element.cc:262-282): element

@@ -108,17 +108,21 @@ struct StagedNodes {
 
 // FP64 form: reference geometry precomputed (geo planes).  FP32 form: the
 // reference Jacobian is rebuilt from X each step with the same transform.
-template <typename T, bool kPrecomputedGeo, class Nodes>
+// kPass: 0 the fused step (F, sigma, records, forces); with a block-material
+// callback the step is split as the reference's plugin path splits it,
+// 1 kinematics (F and the built-in materials' sigma into the records; zero
+// sigma where the callback computes it), 2 forces from the recorded sigma.
+template <typename T, bool kPrecomputedGeo, class Nodes, int kPass = 0>
 __device__ __forceinline__ void element_work(const ElementArgs& a, const int e, const Nodes& nodes);
 
 // One thread per element, or (persistent form) a fixed grid of blocks walking
 // the elements of all samples in tiles of blockDim.x.
-template <typename T, bool kPrecomputedGeo, bool kPersistent, int kMinBlocks = 1>
+template <typename T, bool kPrecomputedGeo, bool kPersistent, int kMinBlocks = 1, int kPass = 0>
 __global__ void __launch_bounds__(128, kMinBlocks) k_element(ElementArgs a)
 {
   if constexpr (!kPersistent) {
     const int e = a.e_begin + blockIdx.x * blockDim.x + threadIdx.x;
-    if (e < a.E) element_work<T, kPrecomputedGeo>(a, e, GlobalNodes<T>(a, e));
+    if (e < a.E) element_work<T, kPrecomputedGeo, GlobalNodes<T>, kPass>(a, e, GlobalNodes<T>(a, e));
   } else {
     for (long e = a.e_begin + blockIdx.x * (long)blockDim.x + threadIdx.x; e < a.E;
          e += (long)gridDim.x * blockDim.x)
@@ -195,7 +199,7 @@ __global__ void __launch_bounds__(128, 3) k_element_staged(ElementArgs a)
   cp_async_wait_all();
 }
 
-template <typename T, bool kPrecomputedGeo, class Nodes>
+template <typename T, bool kPrecomputedGeo, class Nodes, int kPass>
 __device__ __forceinline__ void element_work(const ElementArgs& a, const int e, const Nodes& nodes)
 {
   const long ld_e = a.ld_e;
@@ -241,7 +245,8 @@ __device__ __forceinline__ void element_work(const ElementArgs& a, const int e, 
   bool    bad = false;
   T*      rec = reinterpret_cast<T*>(a.ip) + (size_t)e * kIpRecord;
   const bool store =
-      a.store_ip || (a.sched != nullptr && a.sched[(long)(*a.step_base + a.k) * a.num_groups].is_output);
+      kPass == 1 ||
+      (kPass == 0 && (a.store_ip || (a.sched != nullptr && a.sched[(long)(*a.step_base + a.k) * a.num_groups].is_output)));
   // a warp of 32 consecutive elements stores through its tile; a partial warp lane by lane
   constexpr int kRecChunks = kIpRecord * (int)sizeof(T) / 16, kForceChunks = 24 * (int)sizeof(T) / 16;
   constexpr int kTile      = tile_chunks<kRecChunks>() > tile_chunks<kForceChunks>() ? tile_chunks<kRecChunks>()
@@ -289,8 +294,13 @@ __device__ __forceinline__ void element_work(const ElementArgs& a, const int e, 
     // det J_x = J det J_X, and the force term det(J_x) J_x^{-1} sigma = adj(J_x) sigma
     T       Cx[3][3];
     const T J = cofactor3<T>(Jx, Cx) * idet0;
-    T       sig[6];
-    material_stress_j<T>(model, H, J, K, Gm, sig);
+    T sig[6];
+    if constexpr (kPass == 2) {  // the stress the kinematics pass and the callback recorded
+#pragma unroll
+      for (int q = 0; q < 6; q++) sig[q] = rec[(size_t)p * ld_e * kIpRecord + 9 + q];
+    } else {
+      material_stress_j<T>(model, H, J, K, Gm, sig);
+    }
     if (!positive(J)) bad = true;  // inverted element
     if (store) {
       T r[kIpRecord];
@@ -309,14 +319,20 @@ __device__ __forceinline__ void element_work(const ElementArgs& a, const int e, 
     }
     // Q[d][i] = sum_k adj(J_x)[d][k] sigma[k][i] = sum_k cof(J_x)[k][d] sigma[k][i],
     // summed over the two points of each sign pair (the first assigns)
+    if constexpr (kPass != 1) {
 #pragma unroll
-    for (int d = 0; d < 3; d++)
+      for (int d = 0; d < 3; d++)
 #pragma unroll
-      for (int i = 0; i < 3; i++) {
-        T&      acc  = S[d][i][bit[other1(d)]][bit[other2(d)]];
-        const T tail = first_of_pair(d, p) ? Cx[2][d] * sym(sig, 2, i) : fma(Cx[2][d], sym(sig, 2, i), acc);
-        acc          = fma(Cx[0][d], sym(sig, 0, i), fma(Cx[1][d], sym(sig, 1, i), tail));
-      }
+        for (int i = 0; i < 3; i++) {
+          T&      acc  = S[d][i][bit[other1(d)]][bit[other2(d)]];
+          const T tail = first_of_pair(d, p) ? Cx[2][d] * sym(sig, 2, i) : fma(Cx[2][d], sym(sig, 2, i), acc);
+          acc          = fma(Cx[0][d], sym(sig, 0, i), fma(Cx[1][d], sym(sig, 1, i), tail));
+        }
+    }
+  }
+  if constexpr (kPass == 1) {  // kinematics only: the records are written
+    if (bad) atomicOr(a.status, NSM_STATUS_BAD_JACOBIAN);
+    return;
   }
 
   // f_a,i = - sum_p sum_d dN_a/dxi_d(p) Q_p[d][i].  J_x and hence Q carry
@@ -403,6 +419,25 @@ cudaError_t launch_element_fp64(const ElementArgs& a, const ElementLaunch& l, cu
   return launch_element<double, true>(a, l, stream);
 }
 
+cudaError_t launch_element_pass(const ElementArgs& a, int is_float, int pass, cudaStream_t stream)
+{
+  if (a.E <= a.e_begin) return cudaSuccess;
+  const int grid = grid_for(a.E - a.e_begin, 128);
+  if (pass != 1 && pass != 2) return cudaErrorInvalidValue;
+  if (is_float) {
+    if (pass == 1)
+      k_element<float, false, false, 3, 1><<<grid, 128, 0, stream>>>(a);
+    else
+      k_element<float, false, false, 3, 2><<<grid, 128, 0, stream>>>(a);
+  } else {
+    if (pass == 1)
+      k_element<double, true, false, 1, 1><<<grid, 128, 0, stream>>>(a);
+    else
+      k_element<double, true, false, 1, 2><<<grid, 128, 0, stream>>>(a);
+  }
+  return cudaGetLastError();
+}
+
 cudaError_t launch_element_fp32(const ElementArgs& a, const ElementLaunch& l, cudaStream_t stream)
 {
   if (!l.staged) return launch_element<float, false>(a, l, stream);
@@ -474,8 +509,10 @@ __global__ void __launch_bounds__(128) k_energy_partials(int N, long ld_n, const
           }
           H[i][J] = h;
         }
-      ie += geo[(p * kGeoPerPoint + 9) * ld_e + e] *
-            (elastic_model ? energy_density_elastic(H, K, Gm) : energy_density(H, K, Gm));
+      // (a block whose stress a callback computes has no energy density here)
+      if (mat.model != kExternal)
+        ie += geo[(p * kGeoPerPoint + 9) * ld_e + e] *
+              (elastic_model ? energy_density_elastic(H, K, Gm) : energy_density(H, K, Gm));
     }
   }
   s_ke[threadIdx.x] = ke;

@@ -299,10 +299,14 @@ __device__ __forceinline__ void material_stress(int model, const T H[3][3], T K,
 template <typename T>
 __device__ __forceinline__ void material_stress_j(int model, const T H[3][3], T J, T K, T G, T sig[6])
 {
-  if (model == kElastic)
+  if (model == kElastic) {
     elastic_stress<T>(H, K, G, sig);
-  else
+  } else if (model == kExternal) {  // the block's callback writes it
+#pragma unroll
+    for (int q = 0; q < 6; q++) sig[q] = T(0);
+  } else {
     neohookean_stress<T>(H, J, K, G, sig);
+  }
 }
 
 template <typename T>

@@ -16,6 +16,7 @@ namespace nsm {
 // src/nimble_material_factory.cc:57-70).
 constexpr int kNeohookean = 0;  // "neohookean", src/nimble_material.cc:252-310
 constexpr int kElastic    = 1;  // "elastic", src/nimble_material.cc:98-126
+constexpr int kExternal   = 2;  // computed by a registered block-material callback (the plugin path)
 
 // Natural coordinate of the Gauss points (src/nimble_element.cc:58).
 constexpr double kGauss = 0.577350269189626;

@@ -101,6 +101,10 @@ struct ElementLaunch {
 };
 cudaError_t launch_element_fp64(const ElementArgs& a, const ElementLaunch& l, cudaStream_t stream);
 cudaError_t launch_element_fp32(const ElementArgs& a, const ElementLaunch& l, cudaStream_t stream);
+// The split step of models with a block-material callback: pass 1 the
+// kinematics (F, built-in sigma, records), pass 2 the forces from the
+// recorded sigma (one thread per element).
+cudaError_t launch_element_pass(const ElementArgs& a, int is_float, int pass, cudaStream_t stream);
 int         num_sms();
 // F = I (sigma = 0) in every point record: the element data before the first step.
 cudaError_t launch_ip_identity(int E, long ld_e, void* ip, int ip_is_float, cudaStream_t stream);

@@ -91,6 +91,21 @@ struct nsm_model {
   std::vector<double> dt_group;    // per-sample critical time step
   nsm::ElementLaunch  elaunch{128, 0, 0, 0};
   nsm_mlp*            closure = nullptr;        // learned material (FP32 form), or null
+  // block materials computed by callbacks (the plugin path)
+  struct BlockCallback {
+    nsm_stress_callback fn = nullptr;
+    void*               user = nullptr;
+    int                 num_state = 0;
+  };
+  std::vector<BlockCallback>       block_cb;       // per block (material index)
+  std::vector<nsm::GroupMaterial>  h_mats;         // host copy of the materials, as created
+  std::vector<std::pair<int, int>> block_range;    // elements [first, last) of each block
+  int                              num_state = 0;  // per point, the largest registered
+  void*                            d_ip_n = nullptr;     // records of step n (the split step)
+  double*                          d_state = nullptr;    // [8][ld_e][num_state], latest
+  double*                          d_state_n = nullptr;  // the step before
+  double                           ci_t_prev = 0, ci_t_cur = 0;  // times of a direct internal-force call
+  bool                             cb_failed = false;            // a callback returned nonzero
   float*              d_closure_geo = nullptr;  // [ld_e][8][12] its reference geometry per point
   unsigned long long* d_fallbacks = nullptr;    // points that left the closure's envelope
 
@@ -151,7 +166,7 @@ void free_all(nsm_model* m)
                   m->d_bcs,  m->d_ibc_slot, m->d_ibcs,     m->d_sched, m->d_group_out, m->d_elem_group,
                   m->d_node_group, m->d_elem_off, m->d_mats, m->d_fallbacks, m->d_node_off, m->d_closure,
                   m->d_stage_out, m->d_expr_code, m->d_expr_start, m->d_bc_slot_node, m->d_bc_expr_val,
-                  m->d_closure_geo};
+                  m->d_closure_geo, m->d_ip_n, m->d_state, m->d_state_n};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (cudaStream_t s : m->hp_stream)
@@ -349,8 +364,62 @@ cudaError_t sync_uf(nsm_model* m)
   return nsm::launch_to_float(3 * m->ld_n, m->d_u, m->d_uf, m->stream);
 }
 
+bool has_callbacks(const nsm_model* m)
+{
+  for (const auto& c : m->block_cb)
+    if (c.fn) return true;
+  return false;
+}
+
+// The split step of a model with block-material callbacks: the buffers of
+// steps n and n+1 alternate, the kinematics pass writes F (and the built-in
+// blocks' sigma) at n+1, each callback writes its block's sigma and state,
+// and the forces follow from the recorded sigma.
+cudaError_t element_split(nsm_model* m, int k)
+{
+  std::swap(m->d_ip, m->d_ip_n);
+  std::swap(m->d_state, m->d_state_n);
+  double t_n = m->ci_t_prev, t_np1 = m->ci_t_cur;
+  if (k >= 0) {
+    const size_t s = (size_t)(m->steps_done + k);
+    t_n            = m->h_time[s];
+    t_np1          = m->h_time[s + 1];
+  }
+  const int        is_float = m->precision == NSM_PRECISION_FP64 ? 0 : 1;
+  nsm::ElementArgs a        = element_args(m, k);
+  cudaError_t      e        = nsm::launch_element_pass(a, is_float, 1, m->stream);
+  for (size_t b = 0; b < m->block_cb.size() && e == cudaSuccess; b++) {
+    const auto& cb = m->block_cb[b];
+    if (!cb.fn || m->block_range[b].first < 0) continue;
+    nsm_stress_request r;
+    r.block        = (int)b;
+    r.elem_begin   = m->block_range[b].first;
+    r.elem_end     = m->block_range[b].second;
+    r.precision    = m->precision;
+    r.ld_e         = m->ld_e;
+    r.records_n    = m->d_ip_n;
+    r.records_np1  = m->d_ip;
+    r.num_state    = m->num_state;
+    r.state_n      = m->num_state > 0 ? m->d_state_n : nullptr;
+    r.state_np1    = m->num_state > 0 ? m->d_state : nullptr;
+    r.time_n       = t_n;
+    r.time_np1     = t_np1;
+    r.density      = m->h_mats[b].density;
+    r.bulk_modulus = m->h_mats[b].bulk;
+    r.shear_modulus = m->h_mats[b].shear;
+    r.stream       = m->stream;
+    if (cb.fn(cb.user, &r) != 0) {
+      m->cb_failed = true;
+      return cudaErrorLaunchFailure;  // reported as the callback's failure
+    }
+  }
+  if (e == cudaSuccess) e = nsm::launch_element_pass(a, is_float, 2, m->stream);
+  return e;
+}
+
 cudaError_t launch_element(nsm_model* m, int k)
 {
+  if (has_callbacks(m)) return element_split(m, k);
   nsm::ElementArgs a = element_args(m, k);
   if (m->closure) {
     nsm::mlp::MlpElementArgs ma;
@@ -516,6 +585,9 @@ int create_impl(int S, const nsm_mesh_desc* meshes, int num_mats, const nsm_mate
   for (int b = 0; b < num_mats; b++)
     gm[b] = nsm::GroupMaterial{materials[b].bulk_modulus, materials[b].shear_modulus, materials[b].density,
                                std::sqrt(materials[b].bulk_modulus / materials[b].density), materials[b].model, 0};
+  m->h_mats = gm;
+  m->block_cb.assign(num_mats, nsm_model::BlockCallback{});
+  m->block_range.assign(num_mats, std::make_pair(-1, -1));
 
   auto bail = [&](int code) {
     free_all(m);
@@ -586,6 +658,9 @@ int create_impl(int S, const nsm_mesh_desc* meshes, int num_mats, const nsm_mate
           gconn[8 * ge + c]                = gid;
         }
         if (num_mats > 1) egroup[ge] = elem_mat ? elem_mat[ge] : g;
+        const int b = num_mats > 1 ? egroup[ge] : 0;  // blocks are contiguous (checked above)
+        if (m->block_range[b].first < 0) m->block_range[b].first = (int)ge;
+        m->block_range[b].second = (int)ge + 1;
       }
       for (long n = 0; n < mesh.num_nodes; n++) {
         long gn = node_off[g] + n;
@@ -919,11 +994,16 @@ int nsm_get_node_field(nsm_model* m, int field, double* values)
   return NSM_OK;
 }
 
-int nsm_compute_internal_force(nsm_model* m, double, double, int)
+int nsm_compute_internal_force(nsm_model* m, double time_previous, double time_current, int)
 {
   if (!m) return fail(NSM_ERR_INVALID_ARGUMENT, "null model");
   NSM_CUDA(cudaSetDevice(m->device));
-  NSM_CUDA(launch_element(m, -1));
+  m->ci_t_prev  = time_previous;  // the step's times for block-material callbacks
+  m->ci_t_cur   = time_current;
+  m->cb_failed  = false;
+  cudaError_t e = launch_element(m, -1);
+  if (m->cb_failed) return fail(NSM_ERR_STATE, "a block-material callback failed");
+  NSM_CUDA(e);
   NSM_CUDA(nsm::launch_node_update(node_args(m, -1, -1, 1), m->stream));
   return read_status(m);
 }
@@ -935,7 +1015,7 @@ namespace {
 // forces of other samples' elements) or a small mesh.
 int host_chunk_count(const nsm_model* m)
 {
-  if (m->closure || m->d_closure) return 1;
+  if (m->closure || m->d_closure || has_callbacks(m)) return 1;
   int k = m->host_chunks > 0 ? m->host_chunks : (m->E >= (1 << 18) ? 8 : 1);
   if (k > m->E) k = m->E > 0 ? m->E : 1;
   return k;
@@ -1078,6 +1158,64 @@ int nsm_compute_internal_force_host(nsm_model* m, const double* displacement, do
   return read_status(m);  // synchronizes
 }
 
+int nsm_set_block_material_callback(nsm_model* m, int block, int num_state, nsm_stress_callback fn, void* user)
+{
+  if (!m) return fail(NSM_ERR_INVALID_ARGUMENT, "null model");
+  if (block < 0 || block >= (int)m->block_cb.size()) return fail(NSM_ERR_INVALID_ARGUMENT, "no such block");
+  if (num_state < 0 || num_state > 64) return fail(NSM_ERR_INVALID_ARGUMENT, "0 to 64 state variables per point");
+  if (m->S != 1 || m->d_closure) return fail(NSM_ERR_INVALID_ARGUMENT, "block-material callbacks take single-mesh models");
+  if (m->closure) return fail(NSM_ERR_INVALID_ARGUMENT, "the model has a learned closure");
+  NSM_CUDA(cudaSetDevice(m->device));
+  NSM_CUDA(cudaStreamSynchronize(m->stream));
+  const size_t rec_bytes = m->elem_bytes() * nsm::kIpRecord * 8 * (size_t)m->ld_e;
+  if (fn && !m->d_ip_n) {  // the record buffer of step n: a copy of the current records
+    NSM_CUDA(cudaMalloc(&m->d_ip_n, rec_bytes));
+    NSM_CUDA(cudaMemcpyAsync(m->d_ip_n, m->d_ip, rec_bytes, cudaMemcpyDeviceToDevice, m->stream));
+  }
+  m->block_cb[block] = fn ? nsm_model::BlockCallback{fn, user, num_state} : nsm_model::BlockCallback{};
+  int ns = 0;
+  for (const auto& c : m->block_cb)
+    if (c.fn && c.num_state > ns) ns = c.num_state;
+  if (ns > m->num_state) {  // the state buffers, zero (initial state)
+    const size_t sb = sizeof(double) * 8 * (size_t)m->ld_e * ns;
+    if (m->d_state) cudaFree(m->d_state);
+    if (m->d_state_n) cudaFree(m->d_state_n);
+    m->d_state = m->d_state_n = nullptr;
+    NSM_CUDA(cudaMalloc(&m->d_state, sb));
+    NSM_CUDA(cudaMalloc(&m->d_state_n, sb));
+    NSM_CUDA(cudaMemsetAsync(m->d_state, 0, sb, m->stream));
+    NSM_CUDA(cudaMemsetAsync(m->d_state_n, 0, sb, m->stream));
+    m->num_state = ns;
+  }
+  // the block's material on the device: computed by the callback, or its own again
+  std::vector<nsm::GroupMaterial> mats = m->h_mats;
+  for (size_t b = 0; b < mats.size(); b++)
+    if (m->block_cb[b].fn) mats[b].model = nsm::kExternal;
+  if (m->num_mats == 1) m->model = mats[0].model;
+  NSM_CUDA(cudaMemcpyAsync(m->d_mats, mats.data(), sizeof(nsm::GroupMaterial) * mats.size(), cudaMemcpyHostToDevice,
+                           m->stream));
+  NSM_CUDA(cudaStreamSynchronize(m->stream));
+  for (auto& g : m->graphs) cudaGraphExecDestroy(g.second);  // the step is no longer the fused one
+  m->graphs.clear();
+  return NSM_OK;
+}
+
+int nsm_get_state_data(nsm_model* m, double* state)
+{
+  if (!m || !state) return fail(NSM_ERR_INVALID_ARGUMENT, "null argument");
+  if (m->num_state == 0 || m->E == 0) return NSM_OK;
+  NSM_CUDA(cudaSetDevice(m->device));
+  const int ns = m->num_state;
+  std::vector<double> planes((size_t)8 * m->ld_e * ns);
+  NSM_CUDA(cudaMemcpyAsync(planes.data(), m->d_state, sizeof(double) * planes.size(), cudaMemcpyDeviceToHost,
+                           m->stream));
+  NSM_CUDA(cudaStreamSynchronize(m->stream));
+  for (int e = 0; e < m->E; e++)
+    for (int p = 0; p < 8; p++)
+      for (int k = 0; k < ns; k++) state[((size_t)e * 8 + p) * ns + k] = planes[((size_t)p * m->ld_e + e) * ns + k];
+  return NSM_OK;
+}
+
 int nsm_get_ip_data(nsm_model* m, double* F, double* sigma)
 {
   if (!m) return fail(NSM_ERR_INVALID_ARGUMENT, "null model");
@@ -1182,6 +1320,17 @@ int nsm_begin_ensemble(nsm_model* m, double initial_time, const double* final_ti
   NSM_CUDA(cudaMemsetAsync(m->d_v, 0, nb, m->stream));
   NSM_CUDA(cudaMemsetAsync(m->d_a, 0, nb, m->stream));
   NSM_CUDA(cudaMemsetAsync(m->d_f, 0, nb, m->stream));
+  if (m->d_ip_n) {  // the split step's element data: F = I, sigma = 0 at both levels, zero state
+    const size_t rec_bytes = m->elem_bytes() * nsm::kIpRecord * 8 * (size_t)m->ld_e;
+    const int    is_float  = m->precision == NSM_PRECISION_FP64 ? 0 : 1;
+    for (void* rec : {m->d_ip, m->d_ip_n}) {
+      NSM_CUDA(cudaMemsetAsync(rec, 0, rec_bytes, m->stream));
+      NSM_CUDA(nsm::launch_ip_identity(m->E, m->ld_e, rec, is_float, m->stream));
+    }
+    if (m->num_state > 0)
+      for (double* st : {m->d_state, m->d_state_n})
+        NSM_CUDA(cudaMemsetAsync(st, 0, sizeof(double) * 8 * (size_t)m->ld_e * m->num_state, m->stream));
+  }
   int r = nsm_apply_initial_conditions(m);
   if (r) return r;
   if (v_init) {
@@ -1215,6 +1364,16 @@ int nsm_advance(nsm_model* m, int num_steps)
   NSM_CUDA(cudaSetDevice(m->device));
   int r0 = upload_bcs(m);
   if (r0) return r0;
+  if (has_callbacks(m)) {  // one step at a time without graphs: each callback sees its step's times
+    for (; num_steps > 0; num_steps--) {
+      m->cb_failed  = false;
+      cudaError_t e = enqueue_chunk(m, 1, m->profiling);
+      if (m->cb_failed) return fail(NSM_ERR_STATE, "a block-material callback failed");
+      NSM_CUDA(e);
+      m->steps_done += 1;
+    }
+    return NSM_OK;
+  }
   while (num_steps > 0) {
     int K = num_steps < m->graph_steps ? num_steps : m->graph_steps;
     if (m->profiling) {

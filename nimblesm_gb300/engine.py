@@ -80,6 +80,10 @@ SIGNATURES = {
     "nsm_compute_internal_force": (C.c_int, [_vp, C.c_double, C.c_double, C.c_int]),
     "nsm_compute_internal_force_host": (C.c_int, [_vp, _dp, _dp]),
     "nsm_set_host_chunks": (C.c_int, [_vp, C.c_int]),
+    "nsm_set_block_material_callback": (C.c_int, [_vp, C.c_int, C.c_int, _vp, _vp]),
+    "nsm_get_state_data": (C.c_int, [_vp, _dp]),
+    "nsm_example_neohookean_callback": (C.c_int, [_vp, _vp]),
+    "nsm_example_history_callback": (C.c_int, [_vp, _vp]),
     "nsm_host_chunks": (C.c_int, [_vp, _ip]),
     "nsm_get_ip_data": (C.c_int, [_vp, _dp, _dp]),
     "nsm_compute_derived_element_data": (C.c_int, [_vp, _dp, _dp, _dp]),
@@ -156,6 +160,17 @@ def _add_bc(lib, h, bc, nodes):
     else:
         _check(lib.nsm_add_boundary_condition(h, bc.kind, bc.component, bc.value, nodes.ctypes.data_as(_ip),
                                               len(nodes)))
+
+
+# The block-material callback type (nsm_stress_callback): int fn(void* user,
+# const nsm_stress_request* request).
+STRESS_CALLBACK = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p)
+
+
+def example_callback(name):
+    """The address of one of the library's example block-material callbacks:
+    "neohookean" (stateless) or "history" (one state variable per point)."""
+    return C.cast(getattr(library(), f"nsm_example_{name}_callback"), C.c_void_p).value
 
 
 def bc_expression_eval(expression, x=0.0, y=0.0, z=0.0, t=0.0):
@@ -276,6 +291,23 @@ class Model:
 
     def ComputeInternalForce(self, time_previous=0.0, time_current=0.0, is_output_step=False):
         _check(library().nsm_compute_internal_force(self._h, time_previous, time_current, int(is_output_step)))
+
+    def set_block_material_callback(self, block, fn, num_state=0, user=None):
+        """Block `block`'s stress computed by the callback `fn` (a C function
+        address, or a STRESS_CALLBACK instance kept alive by the caller) with
+        num_state variables per point; fn None restores the block's material."""
+        addr = None if fn is None else (C.cast(fn, C.c_void_p).value if isinstance(fn, STRESS_CALLBACK) else fn)
+        _check(library().nsm_set_block_material_callback(self._h, int(block), int(num_state), addr, user))
+        self._num_state = max(getattr(self, "_num_state", 0), int(num_state)) if fn is not None else \
+            getattr(self, "_num_state", 0)
+
+    def get_state_data(self):
+        """The per-point state after the last step, [E, 8, num_state]."""
+        ns = getattr(self, "_num_state", 0)
+        out = np.zeros((self.problem.num_elem, 8, ns))
+        if ns:
+            _check(library().nsm_get_state_data(self._h, _d(out)))
+        return out
 
     def set_host_chunks(self, chunks):
         """Element ranges of the host-buffer pipeline (0: default)."""

@@ -15,7 +15,7 @@ import os
 
 import numpy as np
 
-from .mesh import BC_PRESCRIBED_DISPLACEMENT, Problem
+from .mesh import BC_PRESCRIBED_DISPLACEMENT, BC_PRESCRIBED_TRACTION, Problem
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_lib", "libnimble_gb300.so")
@@ -153,7 +153,10 @@ def _check(rc):
 
 
 def _add_bc(lib, h, bc, nodes):
-    """One boundary-condition line over its (global) node ids."""
+    """One boundary-condition line over its (global) node ids (a traction line
+    applies nothing, as in the reference)."""
+    if bc.kind == BC_PRESCRIBED_TRACTION:
+        return
     if bc.expression is not None:
         _check(lib.nsm_add_boundary_condition_expression(h, bc.kind, bc.component, bc.expression.encode(),
                                                          nodes.ctypes.data_as(_ip), len(nodes)))

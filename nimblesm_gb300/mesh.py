@@ -17,11 +17,18 @@ import numpy as np
 BC_INITIAL_VELOCITY = 0
 BC_PRESCRIBED_VELOCITY = 1
 BC_PRESCRIBED_DISPLACEMENT = 2
+# A traction line names a side set; the reference parses it and applies
+# nothing (BoundaryConditionManager::ApplyTractionBC is an empty loop,
+# src/nimble_boundary_condition_manager.h:230-247), and so does the engine:
+# no node set carries its name, so the line drops out like any line whose
+# node set is absent.
+BC_PRESCRIBED_TRACTION = 3
 
 _BC_KINDS = {
     "initial_velocity": BC_INITIAL_VELOCITY,
     "prescribed_velocity": BC_PRESCRIBED_VELOCITY,
     "prescribed_displacement": BC_PRESCRIBED_DISPLACEMENT,
+    "prescribed_traction": BC_PRESCRIBED_TRACTION,
 }
 _COMPONENTS = {"x": 0, "y": 1, "z": 2}
 
@@ -135,7 +142,7 @@ class Problem:
         (src/nimble_boundary_condition_manager.cc:67-71)."""
         kinds, comps, vals, ptr, nodes = [], [], [], [0], []
         for bc in self.bcs:
-            if bc.node_set not in self.node_sets:
+            if bc.node_set not in self.node_sets or bc.kind == BC_PRESCRIBED_TRACTION:
                 continue
             if bc.expression is not None:
                 raise ValueError("constant boundary magnitudes only: " + bc.line())

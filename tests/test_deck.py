@@ -114,3 +114,14 @@ def test_run_deck_against_gold(name, tmp_path):
     if "gold:volume" in fx:
         for t in range(T):
             assert exodiff_ok(out["elem:volume"][t], fx["gold:volume"][t], fx["tol:volume"]), t
+
+
+def test_traction_lines_parse_and_drop_out():
+    from nimblesm_gb300.mesh import BC_PRESCRIBED_TRACTION, BoundaryCondition
+    b = BoundaryCondition.parse("prescribed_traction sideset_1 x 2.5e6")
+    assert b.kind == BC_PRESCRIBED_TRACTION and b.line() == "prescribed_traction sideset_1 x 2500000.0"
+    p = cube_problem(2)
+    p.bcs = p.bcs + [BoundaryCondition.parse("prescribed_traction nodelist_1 x 1.0")]
+    kinds = p.bc_arrays()[0]
+    assert BC_PRESCRIBED_TRACTION not in kinds and len(kinds) == 3
+

@@ -127,3 +127,17 @@ def test_partial_warps_and_chunks_against_the_oracle(dims):
     m.set_host_chunks(min(7, p.num_elem))
     assert np.array_equal(m.ComputeInternalForceHost(u), ref)
     m.close()
+
+
+def test_a_traction_line_applies_nothing():
+    """The reference parses prescribed_traction lines and applies nothing
+    (ApplyTractionBC is empty): the run is bitwise the run without the line,
+    also when the line's set name is a node set's."""
+    from nimblesm_gb300.mesh import BoundaryCondition
+    p = cube_problem(4, jitter=0.2, seed=9)
+    q = cube_problem(4, jitter=0.2, seed=9)
+    q.bcs = q.bcs + [BoundaryCondition.parse("prescribed_traction nodelist_2 z 1.0e6")]
+    dt = 0.5 * critical_time_step(p)
+    a, b = E.run(p, 20 * dt, 20), E.run(q, 20 * dt, 20)
+    for k in ("u", "v", "sigma"):
+        assert np.array_equal(a[k], b[k]), k

@@ -154,7 +154,7 @@ __device__ __forceinline__ void gather_force(const NodeArgs& a, int n, double f[
 }
 
 template <typename TF, bool kExact>
-__global__ void __launch_bounds__(256) k_node_update(NodeArgs a)
+__global__ void __launch_bounds__(256, sizeof(TF) == 4 ? 5 : 4) k_node_update(NodeArgs a)
 {
   const int n = a.n_begin + blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= a.N) return;

@@ -78,7 +78,8 @@ class ClockSampler:
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
     def __init__(self, device=0):
-        self.path = tempfile.mktemp(suffix=".csv")
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
         self.proc = None
         self.device = device
 

@@ -386,6 +386,10 @@ def run_ours(args):
 
     reps = Replicas()
     ws, rank, local = reps.world, reps.rank, reps.device
+    if ws > 1:
+        # a scaling run measures the workload on every GPU; the variants are
+        # single-GPU measurements and would only hold the GPUs longer
+        args.variants = False
 
     n = args.n
     problem = cube_problem(n, jitter=0.2, seed=0)

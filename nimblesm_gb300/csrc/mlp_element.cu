@@ -145,7 +145,7 @@ __device__ __forceinline__ int rec_slot(int row, int c)
   return ((row ^ ((row >> 3) & 1)) << 2) + (c ^ ((row >> 1) & 3));
 }
 
-__global__ void __launch_bounds__(128, 5) k_element_mlp(ElementArgs a, MlpElementArgs m)
+__global__ void __launch_bounds__(128, 6) k_element_mlp(ElementArgs a, MlpElementArgs m)
 {
   extern __shared__ __align__(1024) uint8_t sm[];
   __shared__ uint64_t mbar;

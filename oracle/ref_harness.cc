@@ -245,7 +245,7 @@ run_impl(
       for (auto const& line : SplitLines(uq_params)) parser.Set("uq parameters", line);
       parser.Set("uq model", std::string("file ") + uq_samples);
 #else
-      throw std::invalid_argument("this build has no UQ mode");
+      throw std::invalid_argument("library compiled without the UQ mode");
 #endif
     }
 

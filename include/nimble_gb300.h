@@ -54,7 +54,8 @@ extern "C" {
 #define NSM_FIELD_VELOCITY 2
 #define NSM_FIELD_ACCELERATION 3
 #define NSM_FIELD_INTERNAL_FORCE 4
-#define NSM_FIELD_EXTERNAL_FORCE 5
+#define NSM_FIELD_EXTERNAL_FORCE 5   /* zero: ModelData::ComputeExternalForce zeroes it every step
+                                        (src/nimble_model_data.cc:610-618), and a = (f_int + 0) / m */
 
 /* Boundary-condition kinds (BoundaryCondition::BC_TYPE,
  * src/nimble_boundary_condition.h; parsed at src/nimble_boundary_condition.cc:65-144). */

@@ -972,6 +972,8 @@ int nsm_set_node_field(nsm_model* m, int field, const double* values)
   double* dst = field_ptr(m, field);
   if (!dst) return fail(NSM_ERR_INVALID_ARGUMENT, "unknown field");
   if (field == NSM_FIELD_REFERENCE_COORDINATE) return fail(NSM_ERR_INVALID_ARGUMENT, "reference coordinates are fixed");
+  if (field == NSM_FIELD_EXTERNAL_FORCE)  // ModelData::ComputeExternalForce zeroes it every step
+    return fail(NSM_ERR_INVALID_ARGUMENT, "the external force is zero on this path");
   NSM_CUDA(cudaSetDevice(m->device));
   if (m->N == 0) return NSM_OK;
   NSM_CUDA(cudaMemcpyAsync(m->d_stage, values, sizeof(double) * 3 * m->N, cudaMemcpyHostToDevice, m->stream));

@@ -141,3 +141,17 @@ def test_a_traction_line_applies_nothing():
     a, b = E.run(p, 20 * dt, 20), E.run(q, 20 * dt, 20)
     for k in ("u", "v", "sigma"):
         assert np.array_equal(a[k], b[k]), k
+
+
+def test_external_force_is_zero():
+    """ModelData::ComputeExternalForce zeroes the external force every step:
+    the field reads as zero and writing it is refused."""
+    p = cube_problem(3, jitter=0.2, seed=10)
+    m = E.Model(p)
+    dt = 0.5 * critical_time_step(p)
+    m.begin(5 * dt, 5, 0)
+    m.advance(5)
+    assert not np.any(m.GetVectorNodeData("external_force"))
+    with pytest.raises(E.EngineError):
+        m.SetVectorNodeData("external_force", np.ones((p.num_nodes, 3)))
+    m.close()

@@ -355,41 +355,40 @@ __global__ void __launch_bounds__(128, 6) k_element_mlp(ElementArgs a, MlpElemen
 #pragma unroll
         for (int i = 0; i < 3; i++) S[d][i] = det0 * (G0[d][0] * P[i][0] + G0[d][1] * P[i][1] + G0[d][2] * P[i][2]);
     }
-    // contribution to node n: -sum_d dN_n/dxi_d(p) S[d][i]
-    float f[8][3];
+    // Nodal forces in modal form.  dN_n/dxi_d(p) = sgn_d(n) prod_{k != d} (1 + g s_{n,k} t_{p,k}) / 8
+    // (s, t the corner's and the point's signs), so f_n = -sum_p sum_d dN_n/dxi_d(p) S_p[d] is the
+    // inverse Walsh-Hadamard transform, over the element's 8 lanes, of the modes
+    // B_M = -g^(|M|-1)/8 sum_{d in M} A_{d, M\d},  A_{d,M'} = sum_p t_p^M' S_p[d]
+    // (S[d] transformed along the two other axes and summed along d).  Lane p holds mode
+    // M = {axes where p's sign is +}; lane masks 1, 3, 4 flip the x, y, z sign.
+    // (the lane's constants are rebuilt from %laneid here rather than held across the loop)
+    uint32_t lid;
+    asm volatile("mov.u32 %0, %%laneid;" : "=r"(lid));
+    const int   q            = (int)(lid & 7u);
+    const int   pb[3]        = {sx_of(q), sy_of(q), sz_of(q)};
+    const int   msize        = pb[0] + pb[1] + pb[2];
+    const float gk           = msize == 3 ? float(-kGauss * kGauss / 8.0) : (msize == 2 ? float(-kGauss / 8.0) : -0.125f);
+    const float mode_sign[3] = {pb[0] ? -1.0f : 1.0f, pb[1] ? -1.0f : 1.0f, pb[2] ? -1.0f : 1.0f};
+    const float mode_k[3]    = {pb[0] ? gk : 0.0f, pb[1] ? gk : 0.0f, pb[2] ? gk : 0.0f};
 #pragma unroll
-    for (int n = 0; n < 8; n++)
+    for (int ax = 0; ax < 3; ax++) {
+      const int flip = ax == 0 ? 1 : (ax == 1 ? 3 : 4);
 #pragma unroll
-      for (int i = 0; i < 3; i++) {
-        float v = 0.0f;
+      for (int d = 0; d < 3; d++)
 #pragma unroll
-        for (int d = 0; d < 3; d++) {
-          const float wd = w[d][sign_bit(n, other1(d))][sign_bit(n, other2(d))];
-          v              = sign_bit(n, d) ? fmaf(-wd, S[d][i], v) : fmaf(wd, S[d][i], v);
+        for (int i = 0; i < 3; i++) {
+          const float pv = __shfl_xor_sync(0xffffffffu, S[d][i], flip);
+          S[d][i]        = ax == d ? S[d][i] + pv : fmaf(mode_sign[ax], pv, S[d][i]);
         }
-        f[n][i] = v;
-      }
-    // butterfly over the element's 8 lanes: lane p ends with node p's sum
-    float      g4[4][3], g2[2][3], g1[3];
-    const bool hi4 = (p >> 2) & 1, hi2 = (p >> 1) & 1, hi1 = p & 1;
+    }
+    float g1[3];
 #pragma unroll
-    for (int q = 0; q < 4; q++)
+    for (int i = 0; i < 3; i++) g1[i] = fmaf(mode_k[2], S[2][i], fmaf(mode_k[1], S[1][i], mode_k[0] * S[0][i]));
 #pragma unroll
-      for (int i = 0; i < 3; i++) {
-        const float keep = hi4 ? f[4 + q][i] : f[q][i], send = hi4 ? f[q][i] : f[4 + q][i];
-        g4[q][i]         = keep + __shfl_xor_sync(0xffffffffu, send, 4);
-      }
+    for (int ax = 0; ax < 3; ax++) {
+      const int flip = ax == 0 ? 1 : (ax == 1 ? 3 : 4);
 #pragma unroll
-    for (int q = 0; q < 2; q++)
-#pragma unroll
-      for (int i = 0; i < 3; i++) {
-        const float keep = hi2 ? g4[2 + q][i] : g4[q][i], send = hi2 ? g4[q][i] : g4[2 + q][i];
-        g2[q][i]         = keep + __shfl_xor_sync(0xffffffffu, send, 2);
-      }
-#pragma unroll
-    for (int i = 0; i < 3; i++) {
-      const float keep = hi1 ? g2[1][i] : g2[0][i], send = hi1 ? g2[0][i] : g2[1][i];
-      g1[i]            = keep + __shfl_xor_sync(0xffffffffu, send, 1);
+      for (int i = 0; i < 3; i++) g1[i] = fmaf(-mode_sign[ax], __shfl_xor_sync(0xffffffffu, g1[i], flip), g1[i]);
     }
     if (valid) {
       float* fo = reinterpret_cast<float*>(a.fe) + (size_t)e * 24 + 3 * p;

@@ -51,8 +51,10 @@ ELEMENT_TRAFFIC_128 = {"fp64": 2.671848192e9 + 2.499607296e9, "fp32": 0.11915545
 
 
 def algorithmic_bytes(N, E, precision):
-    """Bytes each step must move once (the ModelData contract after every
-    step): nodes read X, u, v, a, m and write u, v, a, f_int (200 B/node);
+    """Bytes each step moves once in the reference's field layout (the
+    ModelData contract after every step): nodes read X, u, v, a, m and write
+    u, v, a, f_int (200 B/node; this engine keeps a and f_int in registers
+    between the steps of one advance and writes them at its end);
     elements read connectivity and write F and sigma per integration point
     (992 B/element in FP64, 512 B in FP32).  The element kernel's share is
     connectivity, F, sigma and the gathered X and u (48 B/node)."""

@@ -188,8 +188,12 @@ __global__ void __launch_bounds__(256, sizeof(TF) == 4 ? 5 : 4) k_node_update(No
     } else {
       gather_force<TF, kExact>(a, n, f);
     }
+    // f_int (and a, below) are read by nothing inside a launch sequence: the
+    // sequence's last launch (k_pre < 0) leaves them for the host's queries
+    if (a.gather_only || a.k_pre < 0) {
 #pragma unroll
-    for (int i = 0; i < 3; i++) a.f_int[i * ld + n] = f[i];
+      for (int i = 0; i < 3; i++) a.f_int[i * ld + n] = f[i];
+    }
     if (a.gather_only) return;
     const StepSched s  = a.sched[(long)(*a.step_base + a.k_post) * a.num_groups + group];
     const double    im = a.inv_mass[n];
@@ -225,7 +229,7 @@ __global__ void __launch_bounds__(256, sizeof(TF) == 4 ? 5 : 4) k_node_update(No
   for (int i = 0; i < 3; i++) {
     a.u[i * ld + n] = u[i];
     a.v[i * ld + n] = v[i];
-    if (a.k_post >= 0) a.a[i * ld + n] = acc[i];
+    if (a.k_post >= 0 && a.k_pre < 0) a.a[i * ld + n] = acc[i];
     if (a.uf != nullptr) a.uf[i * ld + n] = (float)u[i];
   }
 }

@@ -121,13 +121,14 @@ __device__ __forceinline__ void gather_force(const NodeArgs& a, int n, double f[
 {
   const TF* fe    = reinterpret_cast<const TF*>(a.fe);
   TF        fs[3] = {TF(0), TF(0), TF(0)};
-  const int k0 = __ldg(&a.node_ptr[n]), k1 = __ldg(&a.node_ptr[n + 1]);
-  // the first 8 incidences (all of them at a hex mesh's interior node): every
-  // load issued before the first sum, the sums in the same order as below
-  constexpr int kFirst = 8;
-  int           ec[kFirst];
+  // the first 8 incidences (all of them at a hex mesh's interior node) from
+  // the slot-major copy: every load issued before the first sum, the sums in
+  // the same order as the rest from the CSR below
+  constexpr int  kFirst = 8;
+  const bool     more   = (__ldg(&a.node_more[n >> 5]) >> (n & 31)) & 1u;
+  int            ec[kFirst];
 #pragma unroll
-  for (int j = 0; j < kFirst; j++) ec[j] = k0 + j < k1 ? __ldg(&a.node_inc[k0 + j]) : -1;
+  for (int j = 0; j < kFirst; j++) ec[j] = __ldg(&a.node_slots[(long)j * a.ld_n + n]);
   TF x[kFirst][3];
 #pragma unroll
   for (int j = 0; j < kFirst; j++)
@@ -139,7 +140,8 @@ __device__ __forceinline__ void gather_force(const NodeArgs& a, int n, double f[
 #pragma unroll
       for (int i = 0; i < 3; i++) fs[i] = kExact ? TF(__dadd_rn(double(fs[i]), double(x[j][i]))) : fs[i] + x[j][i];
     }
-  for (int k = k0 + kFirst; k < k1; k++) {
+  const int k1 = more ? __ldg(&a.node_ptr[n + 1]) : 0;
+  for (int k = more ? __ldg(&a.node_ptr[n]) + kFirst : 0; k < k1; k++) {
     const int  ec = __ldg(&a.node_inc[k]);
     const long e  = ec >> 3;
     const int  c  = ec & 7;

@@ -133,6 +133,10 @@ struct NodeArgs {
   long              ld_n, ld_e;
   const int*        node_ptr;
   const int*        node_inc;
+  // the first 8 incidences of each node, slot-major [8][ld_n] (-1 past the
+  // node's last), and a bit per node set when it has more (read from node_inc)
+  const int*        node_slots;
+  const unsigned*   node_more;
   const void*       fe;       // element nodal forces (double or float)
   int               fe_is_float;
   const double*     inv_mass;

@@ -62,6 +62,8 @@ struct nsm_model {
   int*    d_conn = nullptr;  // [8][ld_e]
   int*    d_node_ptr = nullptr;
   int*    d_node_inc = nullptr;
+  int*      d_node_slots = nullptr;  // [8][ld_n] first 8 incidences of each node, -1 past its last
+  unsigned* d_node_more  = nullptr;  // bit n: node n has more than 8 incidences
   double* d_X = nullptr;  // node planes [3][ld_n]
   double* d_u = nullptr;
   double* d_v = nullptr;
@@ -160,7 +162,7 @@ void free_all(nsm_model* m)
 {
   for (auto& g : m->graphs) cudaGraphExecDestroy(g.second);
   m->graphs.clear();
-  void* ptrs[] = {m->d_conn, m->d_node_ptr, m->d_node_inc, m->d_X,     m->d_u,         m->d_v,     m->d_a,
+  void* ptrs[] = {m->d_conn, m->d_node_ptr, m->d_node_inc, m->d_node_slots, m->d_node_more, m->d_X,     m->d_u,         m->d_v,     m->d_a,
                   m->d_f,    m->d_fext,     m->d_mass,     m->d_inv_mass, m->d_geo,    m->d_ip,    m->d_Xf,
                   m->d_uf,   m->d_fe,   m->d_status,   m->d_step_base, m->d_scratch, m->d_stage,  m->d_out,   m->d_bc_slot,
                   m->d_bcs,  m->d_ibc_slot, m->d_ibcs,     m->d_sched, m->d_group_out, m->d_elem_group,
@@ -330,6 +332,8 @@ nsm::NodeArgs node_args(nsm_model* m, int k_post, int k_pre, int gather_only)
   a.ld_e        = m->ld_e;
   a.node_ptr    = m->d_node_ptr;
   a.node_inc    = m->d_node_inc;
+  a.node_slots  = m->d_node_slots;
+  a.node_more   = m->d_node_more;
   a.fe          = m->d_fe;
   a.fe_is_float = m->precision == NSM_PRECISION_FP64 ? 0 : 1;
   a.inv_mass    = m->d_inv_mass;
@@ -606,6 +610,8 @@ int create_impl(int S, const nsm_mesh_desc* meshes, int num_mats, const nsm_mate
   NSM_CUDA_B(cudaMalloc(&m->d_conn, sizeof(int) * 8 * m->ld_e));
   NSM_CUDA_B(cudaMalloc(&m->d_node_ptr, sizeof(int) * (N + 1)));
   NSM_CUDA_B(cudaMalloc(&m->d_node_inc, sizeof(int) * (8L * E > 0 ? 8L * E : 1)));
+  NSM_CUDA_B(cudaMalloc(&m->d_node_slots, sizeof(int) * (m->ld_n > 0 ? 8 * m->ld_n : 1)));
+  NSM_CUDA_B(cudaMalloc(&m->d_node_more, sizeof(unsigned) * (m->ld_n > 0 ? (m->ld_n + 31) / 32 : 1)));
   double** nodal[] = {&m->d_X, &m->d_u, &m->d_v, &m->d_a, &m->d_f, &m->d_fext};
   for (double** p : nodal) {
     NSM_CUDA_B(cudaMalloc(p, nb));
@@ -674,6 +680,20 @@ int create_impl(int S, const nsm_mesh_desc* meshes, int num_mats, const nsm_mate
     for (int n = 0; n < N; n++) ptr[n + 1] += ptr[n];
     std::vector<int> fill(ptr.begin(), ptr.end() - 1);
     for (long i = 0; i < 8L * E; i++) inc[fill[gconn[i]]++] = (int)i;
+    // the same incidences, the first 8 of each node slot-major, so that the
+    // node kernel loads them without reading the node's CSR range first
+    std::vector<int>      slots((size_t)8 * m->ld_n, -1);
+    std::vector<unsigned> more((m->ld_n + 31) / 32, 0u);
+    for (int n = 0; n < N; n++) {
+      for (int j = 0; j < 8 && ptr[n] + j < ptr[n + 1]; j++) slots[(size_t)j * m->ld_n + n] = inc[ptr[n] + j];
+      if (ptr[n + 1] - ptr[n] > 8) more[n >> 5] |= 1u << (n & 31);
+    }
+    if (m->ld_n > 0) {
+      NSM_CUDA_B(cudaMemcpyAsync(m->d_node_slots, slots.data(), sizeof(int) * slots.size(), cudaMemcpyHostToDevice,
+                                 m->stream));
+      NSM_CUDA_B(cudaMemcpyAsync(m->d_node_more, more.data(), sizeof(unsigned) * more.size(),
+                                 cudaMemcpyHostToDevice, m->stream));
+    }
     NSM_CUDA_B(cudaMemcpyAsync(m->d_conn, conn_soa.data(), sizeof(int) * conn_soa.size(), cudaMemcpyHostToDevice,
                                m->stream));
     NSM_CUDA_B(cudaMemcpyAsync(m->d_X, X.data(), sizeof(double) * X.size(), cudaMemcpyHostToDevice, m->stream));

@@ -107,6 +107,13 @@ __device__ __forceinline__ void apply_bc(const NodeBC& bc, double delta, const d
   }
 }
 
+// f + 0.0, the zero external force added as the reference adds it, without
+// the FP64 pipe: the sum is f itself except for -0.0, which becomes +0.0.
+__device__ __forceinline__ double plus_zero(double f)
+{
+  return __double_as_longlong(f) == (long long)0x8000000000000000ULL ? 0.0 : f;
+}
+
 // y + s*x, rounded as the reference's two operations or fused.
 template <bool kExact>
 __device__ __forceinline__ double axpy(double s, double x, double y)
@@ -202,7 +209,7 @@ __global__ void __launch_bounds__(256, sizeof(TF) == 4 ? 5 : 4) k_node_update(No
 #pragma unroll
     for (int i = 0; i < 3; i++) {
       // a = (1/m) (f_int + f_ext), f_ext = 0 (src/integrators/explicit_time_integrator.cc:250-257)
-      acc[i] = kExact ? __dmul_rn(im, __dadd_rn(f[i], 0.0)) : im * f[i];
+      acc[i] = kExact ? __dmul_rn(im, plus_zero(f[i])) : im * f[i];
       v[i]   = axpy<kExact>(s.half, acc[i], a.v[i * ld + n]);
       u[i]   = a.u[i * ld + n];
     }

@@ -210,8 +210,9 @@ int nsm_compute_internal_force_host(nsm_model* model, const double* displacement
  * copied in by node ranges ahead of the element launches that need them and
  * f_int copied out by node ranges as soon as their elements are done, so the
  * copies overlap the element kernel (pinned buffers).  The result is bitwise
- * that of one launch.  0 restores the default (8 for 262,144 elements or
- * more, else 1); the learned and UQ closures always run as one chunk. */
+ * that of one launch.  0 restores the default (for 262,144 elements or
+ * more 8 in FP64 and 4 in FP32, else 1); the learned and UQ closures always
+ * run as one chunk. */
 int nsm_set_host_chunks(nsm_model* model, int chunks);
 int nsm_host_chunks(nsm_model* model, int* chunks);
 

@@ -64,6 +64,11 @@ __device__ __forceinline__ void warp_store(uint4* __restrict__ dst, const T* v, 
   }
 }
 
+// Finiteness without the FP64 pipe: an exponent field of all ones is an
+// infinity or a NaN.
+__device__ __forceinline__ bool finite_bits(double x) { return (__double2hiint(x) & 0x7ff00000) != 0x7ff00000; }
+__device__ __forceinline__ bool finite_bits(float x) { return isfinite(x); }
+
 // J > 0 without the FP64 pipe: the sign and magnitude bits of an IEEE number
 // order like a signed integer (a NaN J passes here and is caught as a
 // non-finite force).
@@ -346,7 +351,7 @@ __device__ __forceinline__ void element_work(const ElementArgs& a, const int e, 
 #pragma unroll
     for (int i = 0; i < 3; i++) {
       fv[n * 3 + i] = f[n][i];
-      finite        = finite && isfinite(f[n][i]);
+      finite        = finite & finite_bits(f[n][i]);
     }
   if (whole)
     warp_store<kForceChunks>(reinterpret_cast<uint4*>(reinterpret_cast<T*>(a.fe) + (size_t)e0 * 24), fv, tile, lane);

@@ -188,7 +188,15 @@ __host__ __device__ constexpr bool first_of_pair(int d, int p)
 __device__ __forceinline__ double rcbrt_refined(double J)
 {
   // FP32 seed, then y <- y (1 + e/3 + 2e^2/9) with e = 1 - J y^3 (error O(e^3)).
-  double y  = (double)rcbrtf((float)J);
+  // J goes to FP32 and the seed back to FP64 by their bits, with integer
+  // operations (conversions would take FP64-pipe slots): the exponent is
+  // rebased by 1023 - 127 = 896 and J's mantissa truncated to 23 bits, for J
+  // in the FP32 normal range (any other J gives a meaningless seed, as the
+  // inverted or degenerate element it comes from is flagged).
+  const int      hi = __double2hiint(J);
+  const unsigned lo = (unsigned)__double2loint(J);
+  const unsigned yb = __float_as_uint(rcbrtf(__uint_as_float(((unsigned)(hi - (896 << 20)) << 3) | (lo >> 29))));
+  double         y  = __hiloint2double((int)((yb >> 3) + (896u << 20)), (int)(yb << 29));
   double y3 = y * y * y;
   double e  = fma(-J, y3, 1.0);
   double c  = fma(e, 2.0 / 9.0, 1.0 / 3.0);

@@ -239,7 +239,7 @@ __global__ void __launch_bounds__(256, sizeof(TF) == 4 ? 5 : 4) k_node_update(No
     a.u[i * ld + n] = u[i];
     a.v[i * ld + n] = v[i];
     if (a.k_post >= 0 && a.k_pre < 0) a.a[i * ld + n] = acc[i];
-    if (a.uf != nullptr) a.uf[i * ld + n] = (float)u[i];
+    if (sizeof(TF) == 4 && a.uf != nullptr) a.uf[i * ld + n] = (float)u[i];  // FP32 forms only
   }
 }
 

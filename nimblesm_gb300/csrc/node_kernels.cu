@@ -141,8 +141,14 @@ __device__ __forceinline__ void gather_force(const NodeArgs& a, int n, double f[
   for (int j = 0; j < kFirst; j++)
 #pragma unroll
     for (int i = 0; i < 3; i++) x[j][i] = ec[j] >= 0 ? __ldg(&fe[(long)(ec[j] >> 3) * 24 + (ec[j] & 7) * 3 + i]) : TF(0);
+  // the first sum is 0 + x: x itself but for -0.0 (+0.0), an integer select
+  // rather than an FP64 add in the exact form
+  if (ec[0] >= 0) {
 #pragma unroll
-  for (int j = 0; j < kFirst; j++)
+    for (int i = 0; i < 3; i++) fs[i] = kExact ? TF(plus_zero(double(x[0][i]))) : fs[i] + x[0][i];
+  }
+#pragma unroll
+  for (int j = 1; j < kFirst; j++)
     if (ec[j] >= 0) {
 #pragma unroll
       for (int i = 0; i < 3; i++) fs[i] = kExact ? TF(__dadd_rn(double(fs[i]), double(x[j][i]))) : fs[i] + x[j][i];

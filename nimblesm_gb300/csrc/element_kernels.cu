@@ -312,7 +312,7 @@ __device__ __forceinline__ void element_work(const ElementArgs& a, const int e, 
 #pragma unroll
       for (int i = 0; i < 3; i++)
 #pragma unroll
-        for (int k = 0; k < 3; k++) r[full_slot(i, k)] = (i == k) ? T(1) + H[i][k] : H[i][k];
+        for (int k = 0; k < 3; k++) r[full_slot(i, k)] = (i == k) ? one_plus(H[i][k]) : H[i][k];
 #pragma unroll
       for (int q = 0; q < 6; q++) r[9 + q] = sig[q];
       r[15] = T(0);

@@ -205,6 +205,37 @@ __device__ __forceinline__ double rcbrt_refined(double J)
 // FP32 form: J^{-1/3} = 2^{-log2(J)/3} with the hardware log2/exp2 (about 2 ulp).
 __device__ __forceinline__ float rcbrt_refined(float J) { return exp2f(__log2f(J) * (-1.0f / 3.0f)); }
 
+// 1 + h rounded to nearest even, as the FP64 add gives it, with integer
+// operations for |h| < 1/2 (normal h; the rest takes the FP64 add).  With h =
+// +-m 2^(e-52), m the 53-bit significand and e <= -2: for h > 0 the sum has
+// exponent 0 and significand 2^52 + rne(m 2^e); for h < 0 exponent -1 and
+// 2^53 - rne(m 2^(e+1)) (2^53 is even, so rounding the subtrahend to even
+// rounds the difference to even).  A significand that reaches 2^53 carries
+// into the exponent field, which gives exactly 1.0.
+__host__ __device__ __forceinline__ unsigned long long rne_shift(unsigned long long m, int k)
+{
+  // m / 2^k rounded to nearest even, k >= 1 (m < 2^53)
+  if (k >= 54) return 0;
+  const unsigned long long q = m >> k, r = m & ((1ull << k) - 1), half = 1ull << (k - 1);
+  return q + ((r > half || (r == half && (q & 1))) ? 1 : 0);
+}
+__host__ __device__ __forceinline__ unsigned long long one_plus_bits(unsigned long long hb)
+{
+  const int                exp = (int)((hb >> 52) & 0x7ff) - 1023;
+  const unsigned long long m   = (hb & ((1ull << 52) - 1)) | (1ull << 52);
+  if (hb >> 63)  // 1 - |h|: exponent -1
+    return (1022ull << 52) + ((1ull << 53) - rne_shift(m, -(exp + 1))) - (1ull << 52);
+  return (1023ull << 52) + rne_shift(m, -exp);  // 1 + h: exponent 0
+}
+__device__ __forceinline__ double one_plus(double h)
+{
+  const unsigned long long hb = (unsigned long long)__double_as_longlong(h);
+  const int                be = (int)((hb >> 52) & 0x7ff);  // biased exponent: |h| < 1/2 and normal is 1..1021
+  if (be == 0 || be > 1021) return 1.0 + h;
+  return __longlong_as_double((long long)one_plus_bits(hb));
+}
+__device__ __forceinline__ float one_plus(float h) { return 1.0f + h; }
+
 // Cofactor matrix of M (C[r][c] = cofactor of entry (r, c)) and det M.
 template <typename T>
 __device__ __forceinline__ T cofactor3(const T M[3][3], T C[3][3])

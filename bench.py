@@ -43,8 +43,8 @@ SCHEDULE_STEPS = 2000  # the workload's schedule: dt = 0.5 dt_crit, 2000 steps
 # 87.9 DFMA (2 flops each) + 47.5 DADD + 37.9 DMUL executed per point (ncu on
 # the 64^3 case, profiles/k_element_fp64_cube64.md).  The FP64 pipe issues
 # 2 of these instructions per SM per cycle, whatever their kind.
-FP64_FLOPS_PER_IP = 261.1
-FP64_INSTR_PER_IP = 173.2
+FP64_FLOPS_PER_IP = 258.1
+FP64_INSTR_PER_IP = 170.2
 # DRAM bytes (read + write) of one element launch on the 128^3 cube, from one
 # ncu capture per form (profiles/k_element_traffic_cube128.md).
 ELEMENT_TRAFFIC_128 = {"fp64": 2.703591424e9 + 2.702464768e9, "fp32": 0.119155456e9 + 1.213316608e9}

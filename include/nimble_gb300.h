@@ -335,14 +335,19 @@ int nsm_get_profile(nsm_model* model, double* element_ms_total, int* element_lau
  * length over the bulk wave speed) without any allocation.  All pointers are
  * caller memory the GPU can read or write: coords [N][3], displacement [N][3]
  * (NULL = zero), conn [E][8], dt_out one double.  It runs on `stream` (a
- * cudaStream_t; NULL = the default stream) and returns without waiting.
+ * cudaStream_t of the current device; NULL = the default stream) and returns
+ * without waiting.  With no elements dt_out receives the largest double, as
+ * nsm_critical_time_step gives for an empty model.
  * Its scratch is a fixed array inside this library sized for
  * NSM_NOALLOC_MAX_ELEMENTS elements (8 MiB per GPU, held until the process
  * exits); larger meshes are rejected with NSM_ERR_INVALID_ARGUMENT.  The first
- * call on a device looks up the array's device address; make that first call
- * before any stream capture.  Calls share the array: calls that overlap on the
- * GPU (different streams or threads) race and must be serialised by the
- * caller. */
+ * call on a device looks up the array's device address and keeps it; make
+ * that first call before any stream capture, and do not call it again on a
+ * device after cudaDeviceReset (the kept address belongs to the old context).
+ * Calls share the array: calls that overlap on the GPU (different streams or
+ * threads) race and must be serialised by the caller.  Every error return
+ * sets nsm_last_error(); a CUDA error left pending by the caller's earlier
+ * work is reported as NSM_ERR_CUDA and not cleared. */
 #define NSM_NOALLOC_MAX_ELEMENTS 1048576
 int nsm_critical_time_step_noalloc(int num_nodes, int num_elem, const double* coords, const double* displacement,
                                    const int* conn, double density, double bulk_modulus, double* dt_out,
@@ -408,10 +413,6 @@ int nsm_tc_selftest(int N, int K, const float* A, const float* B, float* D);
  * context stays usable. */
 int nsm_tc_wait_timeout_selftest(long polls, int* timed_out);
 
-/* Diagnostic: the measured FP64 FMA rate of the device in TFLOP/s (16
- * independent DFMA chains per thread, 64 warps per SM, best of 3 timed
- * launches), the roof of the FP64 element kernel. */
-int nsm_fp64_peak_probe(int device, double* tflops);
 /* Number of SMs of the device. */
 int nsm_device_sm_count(int device, int* count);
 

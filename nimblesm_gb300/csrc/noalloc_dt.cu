@@ -17,9 +17,13 @@
 // extent of the element in the configuration X + u.  This file is compiled
 // without FMA contraction, so with u = 0 the result equals nsm_critical_time_step
 // bit for bit.
+#include <atomic>
+#include <cstdio>
+
 #include <cuda_runtime.h>
 
 #include "../../include/nimble_gb300.h"
+#include "nsm_kernels.cuh"
 
 namespace {
 
@@ -28,10 +32,26 @@ constexpr int kMaxBlocks = 1024;
 // The scratch: per-element time steps, then per-block minima.
 __device__ __align__(256) double g_noalloc_scratch[NSM_NOALLOC_MAX_ELEMENTS + kMaxBlocks];
 
-// Device address of g_noalloc_scratch per device, looked up once per device.
-// (In host code the symbol's name is only a stand-in, not a device address.)
-constexpr int kMaxDevices = 64;
-void*         g_scratch_ptr[kMaxDevices] = {nullptr};
+// Device address of g_noalloc_scratch per device, looked up once per device
+// with that device current.  (In host code the symbol's name is only a
+// stand-in, not a device address.)  Atomic, so two host threads making a
+// device's first call at once store the same value without a data race.
+constexpr int      kMaxDevices = 64;
+std::atomic<void*> g_scratch_ptr[kMaxDevices];
+
+int cuda_error(cudaError_t e, const char* where)
+{
+  char msg[256];
+  snprintf(msg, sizeof msg, "nsm_critical_time_step_noalloc: %s: %s", where, cudaGetErrorString(e));
+  return nsm::set_last_error(NSM_ERR_CUDA, msg);
+}
+
+int invalid(const char* why)
+{
+  char msg[256];
+  snprintf(msg, sizeof msg, "nsm_critical_time_step_noalloc: %s", why);
+  return nsm::set_last_error(NSM_ERR_INVALID_ARGUMENT, msg);
+}
 
 __global__ void k_elem_dt(int E, const int* __restrict__ conn, const double* __restrict__ coords,
                           const double* __restrict__ disp, double sound_speed, double* __restrict__ dt_elem)
@@ -89,24 +109,43 @@ extern "C" int nsm_critical_time_step_noalloc(int num_nodes, int num_elem, const
                                               const double* displacement, const int* conn, double density,
                                               double bulk_modulus, double* dt_out, void* stream)
 {
-  if (num_elem < 1 || num_nodes < 1 || !coords || !conn || !dt_out) return NSM_ERR_INVALID_ARGUMENT;
-  if (num_elem > NSM_NOALLOC_MAX_ELEMENTS) return NSM_ERR_INVALID_ARGUMENT;  // beyond the fixed scratch
-  if (!(density > 0.0) || !(bulk_modulus > 0.0)) return NSM_ERR_INVALID_ARGUMENT;
+  if (num_elem < 0 || num_nodes < 0) return invalid("negative node or element count");
+  if (!dt_out) return invalid("null dt_out");
+  if (num_elem > 0 && (!coords || !conn || num_nodes < 1)) return invalid("null mesh array or no nodes");
+  if (num_elem > NSM_NOALLOC_MAX_ELEMENTS) return invalid("more elements than NSM_NOALLOC_MAX_ELEMENTS");
+  if (!(density > 0.0) || !(bulk_modulus > 0.0)) return invalid("density and bulk modulus must be positive");
+  // An error left by earlier work is reported, not cleared: it is the caller's.
+  cudaError_t e = cudaPeekAtLastError();
+  if (e != cudaSuccess) return cuda_error(e, "an earlier CUDA error is pending");
   int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return NSM_ERR_CUDA;
-  if (!g_scratch_ptr[dev]) {
-    void* p = nullptr;
-    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return NSM_ERR_CUDA;
-    g_scratch_ptr[dev] = p;
+  if ((e = cudaGetDevice(&dev)) != cudaSuccess) return cuda_error(e, "cudaGetDevice");
+  if (dev < 0 || dev >= kMaxDevices) return invalid("device ordinal beyond the library's table");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (s) {  // the scratch looked up below is the current device's: the stream must be on it
+    int sdev = -1;
+    if ((e = cudaStreamGetDevice(s, &sdev)) != cudaSuccess) return cuda_error(e, "cudaStreamGetDevice");
+    if (sdev != dev) return invalid("the stream belongs to another device than the current one");
   }
-  double*      dt_elem = static_cast<double*>(g_scratch_ptr[dev]);
+  void* p = g_scratch_ptr[dev].load(std::memory_order_acquire);
+  if (!p) {
+    if ((e = cudaGetSymbolAddress(&p, g_noalloc_scratch)) != cudaSuccess) return cuda_error(e, "cudaGetSymbolAddress");
+    if (!p) return cuda_error(cudaErrorInvalidSymbol, "cudaGetSymbolAddress");
+    g_scratch_ptr[dev].store(p, std::memory_order_release);
+  }
+  double*      dt_elem = static_cast<double*>(p);
   double*      partial = dt_elem + NSM_NOALLOC_MAX_ELEMENTS;
-  cudaStream_t s       = static_cast<cudaStream_t>(stream);
-  const double c       = sqrt(bulk_modulus / density);
-  k_elem_dt<<<(num_elem + 127) / 128, 128, 0, s>>>(num_elem, conn, coords, displacement, c, dt_elem);
-  int blocks = (num_elem + 255) / 256;
+  int          blocks  = (num_elem + 255) / 256;
   if (blocks > kMaxBlocks) blocks = kMaxBlocks;
-  k_block_min<<<blocks, 256, 0, s>>>(num_elem, dt_elem, partial);
+  if (num_elem > 0) {
+    const double c = sqrt(bulk_modulus / density);
+    k_elem_dt<<<(num_elem + 127) / 128, 128, 0, s>>>(num_elem, conn, coords, displacement, c, dt_elem);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_error(e, "k_elem_dt launch");
+    k_block_min<<<blocks, 256, 0, s>>>(num_elem, dt_elem, partial);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_error(e, "k_block_min launch");
+  }
+  // With no elements the minimum over nothing is the largest double, the value
+  // nsm_critical_time_step gives an empty model.
   k_block_min<<<1, 256, 0, s>>>(blocks, partial, dt_out);
-  return cudaGetLastError() == cudaSuccess ? NSM_OK : NSM_ERR_CUDA;
+  if ((e = cudaGetLastError()) != cudaSuccess) return cuda_error(e, "k_block_min launch");
+  return NSM_OK;
 }

@@ -202,4 +202,8 @@ cudaError_t launch_node_soa_to_aos(int N, long ld_n, const double* src, double* 
 cudaError_t launch_node_aos_to_soa(int N, long ld_n, const double* src, double* dst, float* dstf,
                                    cudaStream_t stream);
 
+// Records the calling thread's nsm_last_error() text and returns `code`
+// (for entry points defined outside nsm_model.cu).
+int set_last_error(int code, const char* msg);
+
 }  // namespace nsm

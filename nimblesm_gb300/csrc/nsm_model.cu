@@ -507,6 +507,8 @@ int get_graph(nsm_model* m, int K, cudaGraphExec_t* out)
 
 }  // namespace
 
+int nsm::set_last_error(int code, const char* msg) { return fail(code, msg); }
+
 extern "C" {
 
 const char* nsm_last_error(void) { return g_error.c_str(); }
@@ -1637,6 +1639,13 @@ int nsm_get_profile(nsm_model* m, double* element_ms_total, int* element_launche
   m->ev_elem_used = 0;
   m->ev_node_used = 0;
   return NSM_OK;
+}
+
+int nsm_device_sm_count(int device, int* count)
+{
+  if (!count) return fail(NSM_ERR_INVALID_ARGUMENT, "null count");
+  cudaError_t e = cudaDeviceGetAttribute(count, cudaDevAttrMultiProcessorCount, device);
+  return e == cudaSuccess ? NSM_OK : cuda_fail(e, "cudaDeviceGetAttribute");
 }
 
 void* nsm_host_alloc(size_t bytes)

@@ -40,13 +40,13 @@ METRIC = "hex8 IP stress updates/sec, plain FP64 vs mixed/MLP at <=1e-3 rel. dis
 UNIT = "IP-updates/s"
 SCHEDULE_STEPS = 2000  # the workload's schedule: dt = 0.5 dt_crit, 2000 steps
 # FP64 work per integration point of the FP64 element kernel's formulation:
-# 87.9 DFMA (2 flops each) + 47.5 DADD + 37.9 DMUL executed per point (ncu on
-# the 64^3 case, profiles/k_element_fp64_cube64.md).  The FP64 pipe issues
-# 2 of these instructions per SM per cycle, whatever their kind.
+# 87.9 DFMA (2 flops each) + 44.5 DADD + 37.9 DMUL executed per point (counted
+# by ncu on the 64^3 case).  The FP64 pipe issues 2 of these instructions per
+# SM per cycle, whatever their kind.
 FP64_FLOPS_PER_IP = 258.1
 FP64_INSTR_PER_IP = 170.2
 # DRAM bytes (read + write) of one element launch on the 128^3 cube, from one
-# ncu capture per form (profiles/k_element_traffic_cube128.md).
+# ncu capture per form.
 ELEMENT_TRAFFIC_128 = {"fp64": 2.703591424e9 + 2.702464768e9, "fp32": 0.119155456e9 + 1.213316608e9}
 
 
@@ -127,6 +127,14 @@ class ClockSampler:
         return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": reasons, "samples": len(rows)}
 
 
+def workload_config(n, problem, ws):
+    """The workload's description, the same dict in both arms."""
+    return {"workload": f"hex8 neo-Hookean explicit step, jittered {n}^3 cube (±20% interior jitter), "
+                        f"dt = 0.5 dt_crit, {SCHEDULE_STEPS}-step schedule",
+            "elements": problem.num_elem, "nodes": problem.num_nodes, "parallelism": f"replicas{ws}",
+            "l2": "inputs larger than L2 (per-step traffic >> 129 MB)"}
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -192,8 +200,7 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * secs / steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"hex8 neo-Hookean explicit step, jittered {n}^3 cube (±20% interior jitter), dt = 0.5 dt_crit",
-                   "elements": problem.num_elem, "nodes": problem.num_nodes, "steps_requested": args.steps},
+        "config": workload_config(n, problem, ws), "steps_requested": args.steps,
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{steps} full steps of the {n}^3 mesh"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -459,38 +466,46 @@ def run_ours(args):
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
         "data": "synthetic",
-        "config": {"workload": f"hex8 neo-Hookean explicit step, jittered {n}^3 cube (±20% interior jitter), dt = 0.5 dt_crit, "
-                               f"{args.precision}", "elements": E_, "nodes": N, "ips_per_step": 8 * E_,
-                   "dt": dt, "schedule_steps": sched, "parallelism": f"replicas{ws}",
-                   "l2": "inputs larger than L2 (per-step traffic >> 129 MB)"},
+        "config": workload_config(n, problem, ws),
+        "form": args.precision, "ips_per_step": 8 * E_, "dt": dt, "schedule_steps": sched,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 24 * N, "d2h_bytes_per_step": 24 * N,
                 "path": "nsm_compute_internal_force_host (pinned u in, f_int out)", "steps": e2e_steps,
                 "host_chunks": m.host_chunks()},
         "gpu_launches": head["launches"],
-        "roofline": {"bound": "hbm", "kernel": "k_element", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "peak_source": peak_kind,
-                     "traffic": ELEMENT_TRAFFIC_128.get(args.precision) if n == 128 else None,
-                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, one 128^3 launch"
-                     if n == 128 else None,
-                     "algorithmic_bytes_per_launch": elem_bytes, "launch_ms": elem_ms, "node_launch_ms": node_ms,
-                     "step_algorithmic_bytes": step_bytes},
         "clocks": head["clocks"],
     }
+    hbm_roof = {"bound": "hbm", "kernel": "k_element<double>" if args.precision == "fp64" else "k_element_staged",
+                "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "peak_source": peak_kind,
+                "traffic": ELEMENT_TRAFFIC_128.get(args.precision) if n == 128 else None,
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, one 128^3 launch"
+                if n == 128 else None,
+                "algorithmic_bytes_per_launch": elem_bytes, "launch_ms": elem_ms, "node_launch_ms": node_ms,
+                "step_algorithmic_bytes": step_bytes}
     if args.precision == "fp64":
-        # the roof that binds the FP64 element kernel: the FP64 pipe
-        peak64 = E.fp64_peak_tflops(local)
-        ach64 = FP64_FLOPS_PER_IP * 8 * E_ / (elem_ms * 1e-3) / 1e12
+        # The FP64 element kernel is bound by the FP64 pipe, not by HBM: its
+        # roofline is the pipe's rate, 2 FP64 instructions (a DFMA counting 2
+        # flops) per SM per cycle at the maximum SM clock.  MEASURED_PEAKS.json
+        # holds no FP64 figure, so the peak is that nominal rate.  The HBM
+        # fraction of the same launch is reported beside it (roofline_hbm).
         sms = E.device_sm_count(local)
         max_mhz = (head["clocks"] or {}).get("sm_max_mhz") or 2070.0
-        nominal = 2 * 2 * sms * max_mhz * 1e6 / 1e12  # 2 DFMA (4 flops) per SM per cycle at the maximum clock
+        nominal = 2 * 2 * sms * max_mhz * 1e6 / 1e12
+        ach64 = FP64_FLOPS_PER_IP * 8 * E_ / (elem_ms * 1e-3) / 1e12
         instr_rate = FP64_INSTR_PER_IP * 8 * E_ / (elem_ms * 1e-3)
-        pipe_rate = 2 * sms * max_mhz * 1e6  # FP64 instructions per second the pipe issues
-        line["roofline_fp64"] = {"bound": "fp64", "kernel": "k_element", "achieved": ach64, "peak": peak64,
-                                 "unit": "TFLOP/s", "frac": ach64 / peak64, "peak_source": "measured (DFMA probe)",
-                                 "peak_nominal": nominal, "frac_nominal": ach64 / nominal,
-                                 "flops_per_ip": FP64_FLOPS_PER_IP, "fp64_instructions_per_ip": FP64_INSTR_PER_IP,
-                                 "pipe_instruction_frac": instr_rate / pipe_rate,
-                                 "flops_source": "executed DFMA/DADD/DMUL per point, ncu (FMA = 2 flops)"}
+        pipe_rate = 2 * sms * max_mhz * 1e6
+        line["roofline"] = {"bound": "fp64", "kernel": "k_element<double>", "achieved": ach64, "peak": nominal,
+                            "unit": "TFLOP/s", "frac": ach64 / nominal,
+                            "peak_source": f"nominal FP64 pipe: 2 DFMA per SM per cycle x {sms} SMs x {max_mhz:.0f} MHz",
+                            "traffic": hbm_roof["traffic"], "traffic_source": hbm_roof["traffic_source"],
+                            "launch_ms": elem_ms, "flops_per_ip": FP64_FLOPS_PER_IP,
+                            "fp64_instructions_per_ip": FP64_INSTR_PER_IP,
+                            "pipe_instruction_frac": instr_rate / pipe_rate,
+                            "flops_source": "executed DFMA/DADD/DMUL per point, ncu (FMA = 2 flops)",
+                            "hbm_frac": hbm_roof["frac"]}
+        line["roofline_hbm"] = hbm_roof
+    else:
+        line["roofline"] = hbm_roof
     variants = {}
     for prec, r in results.items():
         if prec == args.precision:

@@ -123,7 +123,6 @@ SIGNATURES = {
     "nsm_closure_fallbacks": (C.c_int, [_vp, C.POINTER(C.c_ulonglong)]),
     "nsm_tc_selftest": (C.c_int, [C.c_int, C.c_int, _dp_f, _dp_f, _dp_f]),
     "nsm_tc_wait_timeout_selftest": (C.c_int, [C.c_long, C.POINTER(C.c_int)]),
-    "nsm_fp64_peak_probe": (C.c_int, [C.c_int, _dp]),
     "nsm_device_sm_count": (C.c_int, [C.c_int, C.POINTER(C.c_int)]),
     "nsm_host_alloc": (_vp, [C.c_size_t]),
     "nsm_host_free": (None, [_vp]),
@@ -595,13 +594,6 @@ def _concatenate(problems):
     return Problem(coords=coords, conn=conn, node_sets={}, density=problems[0].density,
                    bulk_modulus=problems[0].bulk_modulus, shear_modulus=problems[0].shear_modulus, bcs=[],
                    v_init=v0)
-
-
-def fp64_peak_tflops(device=0):
-    """Measured FP64 FMA rate of the device (TFLOP/s)."""
-    t = C.c_double(0.0)
-    _check(library().nsm_fp64_peak_probe(device, C.byref(t)))
-    return t.value
 
 
 def device_sm_count(device=0):

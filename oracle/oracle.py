@@ -20,7 +20,11 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "_build", "libnsm_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libnimble_ref.so")
-REF_SRC = "/root/reference/src"
+# The reference checkout whose sources oracle/Makefile compiles: the
+# NIMBLESM_REFERENCE environment variable, else where this container mounts it.
+# Where it is absent, only the C restatement is built.
+REF_ROOT = os.environ.get("NIMBLESM_REFERENCE", "/root/reference")
+REF_SRC = os.path.join(REF_ROOT, "src")
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
@@ -41,7 +45,7 @@ def build(ref: bool | None = None) -> None:
     if ref is None:
         ref = os.path.isdir(REF_SRC)
     if ref:
-        subprocess.run(["make", "-s", "-j8", "-C", HERE, "ref"], check=True)
+        subprocess.run(["make", "-s", "-j8", "-C", HERE, "ref", "REF=" + REF_SRC], check=True)
 
 
 class _Model(C.Structure):
@@ -261,12 +265,13 @@ def ref_eval_expression(text, x, y, z, t):
     return v.value
 
 
-def run_ref_outputs(problem, final_time, num_steps, output_frequency=0, with_ip=True):
+def run_ref_outputs(problem, final_time, num_steps, output_frequency=0, with_ip=True, lib=None):
     """Runs the reference itself (oracle/_ref) and returns its state after
     every output step of the schedule (after the last step only when
     output_frequency is 0): a list of dicts like run_port's, F and sigma being
-    the element data the reference stored in that step."""
-    lib = ref()
+    the element data the reference stored in that step.  `lib`: another build
+    of the same harness (the adapter test's), default the reference's."""
+    lib = lib or ref()
     names = list(problem.node_sets.keys())
     ns_ptr = np.zeros(len(names) + 1, np.int32)
     parts = []

@@ -3,8 +3,9 @@
  *
  * TEST INFRASTRUCTURE ONLY.  This file is the checker, never the product: it
  * is linked only into oracle/_ref/libnimble_ref.so and is loaded only by the
- * tests, by tests/golden/make_golden.py and by the CPU-baseline leg of
- * bench.py.
+ * tests and by tests/golden/make_golden.py.  (bench.py's CPU baseline is the
+ * C restatement, oracle/nsm_oracle.c, which is bitwise this code's result and
+ * builds on any host.)
  *
  * What it runs is the reference's code: nimble::DataManager,
  * nimble::ModelData, nimble::Block, nimble::HexElement and

@@ -31,7 +31,7 @@ from nimblesm_gb300.deck import read_deck as parse_deck  # noqa: E402
 from nimblesm_gb300.deck import read_genesis  # noqa: E402
 from oracle import oracle as O  # noqa: E402
 
-REF = "/root/reference"
+REF = O.REF_ROOT  # the reference checkout (NIMBLESM_REFERENCE)
 
 
 def read_exodus(path):
@@ -177,6 +177,90 @@ def ref_envelope_fixture(name, n, jitter, seed, steps):
           "envelope_sigma": rel(rq["sigma"], r["sigma"])}
     np.savez_compressed(os.path.join(HERE, f"ref_{name}.npz"), **fx)
     print("wrote", name, {k: fx[k] for k in fx if str(k).startswith("envelope")})
+
+
+def ref_schedule_fixture(name, n, jitter, seed, steps, threads=8, node_sample=10_000, elem_sample=2_048):
+    """The jittered n^3 cube over its whole schedule (Δt = 0.5 Δt_crit,
+    `steps` steps), too large to commit whole, as seeded subsets plus
+    whole-field figures:
+
+      * u, v, a, f_int at `node_sample` seeded nodes; F and σ of every point of
+        `elem_sample` seeded elements;
+      * whole-field 2-norms of u, v, a, f_int, F and σ, per-z-layer sums of u and
+        v (129 layers for n = 128: every node enters one) and of the element-mean
+        σ (every element enters one), kinetic and internal energy;
+      * the reference's own sensitivity: the same run with the initial velocity
+        perturbed by one ulp (relative 2^-52, seeded signs, as in
+        ref_cube_fixture), compared on the whole fields and on each stored
+        subset and aggregate (`env_*`).
+
+    The runs use the C restatement on `threads` host threads.  Its assembly
+    order is the reference's serial order at any thread count, and it is
+    bitwise the reference's own code on every committed fixture; on this mesh
+    that is checked again here: the reference (oracle/_ref) and the restatement
+    are run for 2 steps of the same schedule and must agree bit for bit."""
+    p = cube_problem(n, jitter=jitter, seed=seed)
+    dt = 0.5 * critical_time_step(p)
+    final_time = steps * dt
+    # the restatement is the reference on this mesh: 2 steps of Δt, both codes
+    rs = O.run_ref(p, 2 * dt, 2, 0)
+    ps = O.run_port(p, 2 * dt, 2, 0, threads=threads)
+    for k in ("u", "v", "a", "f_int", "F", "sigma", "mass"):
+        assert np.array_equal(ps[k], rs[k]), f"restatement differs from the reference in {k} at {n}^3"
+    assert ps["dt_crit"] == rs["dt_crit"]
+    dt_crit = rs["dt_crit"]
+    del ps, rs
+    print("restatement == reference after 2 steps at", n)
+
+    def run(problem):
+        pr = O.PortRun(problem, threads=threads)
+        pr.begin(final_time, steps, 0)
+        secs = pr.advance(steps)
+        st = pr.state()
+        print("  run", steps, "steps", secs, "s")
+        return st
+
+    r = run(p)
+    q = cube_problem(n, jitter=jitter, seed=seed)
+    rng = np.random.default_rng(77)
+    q.v_init = q.v_init * (1.0 + rng.choice([-1.0, 1.0], size=q.v_init.shape) * 2.0 ** -52)
+    rq = run(q)
+
+    rng = np.random.default_rng(20261204)
+    nodes = np.sort(rng.choice(p.num_nodes, node_sample, replace=False))
+    elems = np.sort(rng.choice(p.num_elem, elem_sample, replace=False))
+    zl = np.rint(p.coords[:, 2] * n).astype(np.int64)          # boundary planes stay planar
+    ez = zl[p.conn].min(axis=1)                                 # element layer: its lowest node plane
+
+    def aggregates(st):
+        out = {}
+        for k in ("u", "v", "a", "f_int"):
+            out[k] = st[k][nodes]
+            out[k + "_norm"] = np.linalg.norm(st[k])
+        out["F"], out["sigma"] = st["F"][elems], st["sigma"][elems]
+        out["F_norm"], out["sigma_norm"] = np.linalg.norm(st["F"]), np.linalg.norm(st["sigma"])
+        for k in ("u", "v"):
+            s = np.zeros((n + 1, 3))
+            np.add.at(s, zl, st[k])
+            out[k + "_layer_sum"] = s
+        s = np.zeros((n, 6))
+        np.add.at(s, ez, st["sigma"].mean(axis=1))
+        out["sigma_layer_sum"] = s
+        out["kinetic_energy"], out["internal_energy"] = st["kinetic_energy"], st["internal_energy"]
+        return out
+
+    a, b = aggregates(r), aggregates(rq)
+    rel = lambda x, y: float(np.linalg.norm(np.asarray(x) - np.asarray(y)) / np.linalg.norm(y))
+    fx = {"n": n, "jitter": jitter, "seed": seed, "steps": steps, "final_time": final_time,
+          "dt_crit": dt_crit,
+          "node_index": nodes, "elem_index": elems, **a}
+    for k in ("u", "v", "a", "f_int", "F", "sigma"):
+        fx["envelope_" + k] = rel(rq[k], r[k])          # whole field
+        fx["env_" + k] = rel(b[k], a[k])                # the stored subset
+    for k in ("u_layer_sum", "v_layer_sum", "sigma_layer_sum", "kinetic_energy", "internal_energy"):
+        fx["env_" + k] = rel(b[k], a[k])
+    np.savez_compressed(os.path.join(HERE, f"ref_{name}.npz"), **fx)
+    print("wrote", name, {k: fx[k] for k in fx if str(k).startswith("env")})
 
 
 def ref_derived_fixture(name="cube4_jitter"):
@@ -382,7 +466,8 @@ def ref_bc_expression_run_fixture(steps=300, output_frequency=50):
     print("wrote bc expression run", fx["u"].shape)
 
 
-GENERATORS = {"bc_expressions": lambda: (ref_bc_expressions_fixture(), ref_bc_expression_run_fixture())}
+GENERATORS = {"bc_expressions": lambda: (ref_bc_expressions_fixture(), ref_bc_expression_run_fixture()),
+              "cube128_schedule": lambda: ref_schedule_fixture("cube128_schedule", 128, 0.2, 0, 2000)}
 
 
 if __name__ == "__main__":
@@ -400,3 +485,4 @@ if __name__ == "__main__":
     ref_envelope_fixture("cube40_schedule", 40, 0.2, 0, 2000)
     ref_derived_fixture("cube4_jitter")
     ref_uq_fixture("uq_wave")
+    ref_schedule_fixture("cube128_schedule", 128, 0.2, 0, 2000)

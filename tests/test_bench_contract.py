@@ -36,6 +36,7 @@ def _check_base(d):
 
 def test_reference_arm_line():
     d = _run(["--impl", "reference", "--n", "8", "--steps", "2", "--warmup", "3"], timeout=600)
+    assert d["config"]["elements"] == 512 and d["config"]["parallelism"] == "replicas1"
     _check_base(d)
     assert d["impl"] == "reference" and d["cpu_baseline"]["value"] == d["value"]
     assert d["cpu_baseline"]["kind"] in ("port", "reference") and d["cpu_baseline"]["cores"] >= 1
@@ -49,9 +50,15 @@ def test_our_arm_line():
     assert d["n_gpus"] == 1 and d["dtype"] == "f64"
     assert d["e2e"]["h2d_bytes_per_step"] == 24 * d["config"]["nodes"] == d["e2e"]["d2h_bytes_per_step"]
     assert d["gpu_launches"] > 0
+    # the FP64 element kernel's binding roof is the FP64 pipe; its HBM figure beside it
     r = d["roofline"]
-    assert r["bound"] == "hbm" and r["unit"] == "GB/s" and r["peak"] > 0
-    assert abs(r["frac"] - r["achieved"] / r["peak"]) < 1e-12 and "traffic" in r
-    assert d["roofline_fp64"]["bound"] == "fp64" and 0 < d["roofline_fp64"]["pipe_instruction_frac"] < 1.5
+    assert r["bound"] == "fp64" and r["unit"] == "TFLOP/s" and r["peak"] > 0 and "traffic" in r
+    assert abs(r["frac"] - r["achieved"] / r["peak"]) < 1e-12 and 0 < r["pipe_instruction_frac"] < 1.5
+    h = d["roofline_hbm"]
+    assert h["bound"] == "hbm" and h["unit"] == "GB/s" and h["peak"] > 0
+    assert abs(h["frac"] - h["achieved"] / h["peak"]) < 1e-12 and "traffic" in h
+    # both arms describe the workload with the same dict
+    ref = _run(["--impl", "reference", "--n", "16", "--steps", "1", "--warmup", "3"], timeout=600)
+    assert ref["config"] == d["config"]
     assert d["cpu_baseline"]["value"] > 0 and d["cpu_baseline"]["cores"] >= 1
     assert "sm_mhz" in d["clocks"] and "reasons" in d["clocks"]

@@ -927,6 +927,17 @@ nsm_oracle_get_state(const nsm_oracle* o, double* u, double* v, double* a, doubl
   if (mass) memcpy(mass, o->w.mass, (size_t)m->num_nodes * sizeof(double));
 }
 
+/* ModelData::ComputeInternalForce (src/nimble_model_data.cc:620-667) of the
+ * displacement u alone: f_int [N][3] out; F and sigma of every point are kept
+ * in the handle (nsm_oracle_get_state).  0, or -1 on a non-positive Jacobian. */
+int
+nsm_oracle_internal_force(nsm_oracle* o, const double* u, double* f_int)
+{
+  o->w.bad_jacobian = 0;
+  internal_force(&o->w, u, f_int, o->num_threads);
+  return o->w.bad_jacobian ? -1 : 0;
+}
+
 void
 nsm_oracle_set_state(nsm_oracle* o, const double* u, const double* v, const double* a)
 {

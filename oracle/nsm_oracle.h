@@ -175,6 +175,10 @@ int         nsm_oracle_advance(nsm_oracle* o, int k, double* loop_seconds); /* n
 double      nsm_oracle_time(const nsm_oracle* o);
 void        nsm_oracle_get_state(const nsm_oracle* o, double* u, double* v, double* a, double* f_int, double* F,
                                  double* sigma, double* mass);
+/* The internal force of displacement u [N][3] alone (ModelData::ComputeInternalForce,
+ * src/nimble_model_data.cc:620-667) into f_int [N][3]; F and sigma of every
+ * point are kept for nsm_oracle_get_state.  0, or -1 on a non-positive Jacobian. */
+int         nsm_oracle_internal_force(nsm_oracle* o, const double* u, double* f_int);
 void        nsm_oracle_set_state(nsm_oracle* o, const double* u, const double* v, const double* a);
 void        nsm_oracle_energies(const nsm_oracle* o, double* kinetic, double* internal);
 

@@ -20,14 +20,14 @@ __device__ __forceinline__ void store_vec(double* dst, const double* v, int n)
   for (int k = 0; k < n; k += 2) *reinterpret_cast<double2*>(dst + k) = make_double2(v[k], v[k + 1]);
 }
 
-// Warp-cooperative stores.  A thread's point record (64 or 128 B) and its
-// element forces (96 or 192 B) are contiguous, and so are those of the 32
-// consecutive elements of a warp; stored lane by lane, each store instruction
-// would scatter 16-byte pieces a record apart, which HBM takes at half the
-// rate of contiguous writes.  Instead the warp passes its 32 blocks through a
-// shared-memory tile and each instruction writes 512 contiguous bytes.  The
-// tile slots are swizzled (4 and 8 chunks per block) or padded (6 and 12) so
-// that neither the per-lane writes nor the transposed reads conflict on banks.
+// Warp-cooperative stores.  A thread's point record (64 or 128 B) is
+// contiguous, and so are those of the 32 consecutive elements of a warp;
+// stored lane by lane, each store instruction would scatter 16-byte pieces a
+// record apart, which HBM takes at half the rate of contiguous writes.
+// Instead the warp passes its 32 records through a shared-memory tile and
+// each instruction writes 512 contiguous bytes.  The tile slots are swizzled
+// (4 and 8 chunks per record) so that neither the per-lane writes nor the
+// transposed reads conflict on banks.
 template <int kChunks>
 __device__ __forceinline__ int tile_slot(int row, int c)
 {
@@ -253,9 +253,8 @@ __device__ __forceinline__ void element_work(const ElementArgs& a, const int e, 
       kPass == 1 ||
       (kPass == 0 && (a.store_ip || (a.sched != nullptr && a.sched[(long)(*a.step_base + a.k) * a.num_groups].is_output)));
   // a warp of 32 consecutive elements stores through its tile; a partial warp lane by lane
-  constexpr int kRecChunks = kIpRecord * (int)sizeof(T) / 16, kForceChunks = 24 * (int)sizeof(T) / 16;
-  constexpr int kTile      = tile_chunks<kRecChunks>() > tile_chunks<kForceChunks>() ? tile_chunks<kRecChunks>()
-                                                                                       : tile_chunks<kForceChunks>();
+  constexpr int kRecChunks = kIpRecord * (int)sizeof(T) / 16;
+  constexpr int kTile      = tile_chunks<kRecChunks>();
   __shared__ uint4 tiles[4][kTile];  // blocks of at most 128 threads
   const int        lane   = threadIdx.x & 31;
   const long       e0     = (long)e - lane;  // the warp's elements are e0 .. e0 + 31
@@ -353,10 +352,12 @@ __device__ __forceinline__ void element_work(const ElementArgs& a, const int e, 
       fv[n * 3 + i] = f[n][i];
       finite        = finite & finite_bits(f[n][i]);
     }
-  if (whole)
-    warp_store<kForceChunks>(reinterpret_cast<uint4*>(reinterpret_cast<T*>(a.fe) + (size_t)e0 * 24), fv, tile, lane);
-  else
-    store_vec(reinterpret_cast<T*>(a.fe) + (size_t)e * 24, fv, 24);
+  // corner-major planes fe[(3 c + i) ld_e + e]: each store instruction writes
+  // 32 consecutive elements of one plane, and the node kernel's gather of a
+  // row of nodes reads 32 consecutive elements of one plane
+  T* fe = reinterpret_cast<T*>(a.fe) + e;
+#pragma unroll
+  for (int q = 0; q < 24; q++) fe[(size_t)q * ld_e] = fv[q];
   if (bad || !finite) atomicOr(a.status, (bad ? NSM_STATUS_BAD_JACOBIAN : 0) | (finite ? 0 : NSM_STATUS_NONFINITE));
 }
 

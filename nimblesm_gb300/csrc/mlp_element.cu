@@ -282,7 +282,7 @@ __global__ void __launch_bounds__(128, 6) k_element_mlp(ElementArgs a, MlpElemen
         float L[6], xs[9];
 #pragma unroll
         for (int q = 0; q < 9; q++) xs[q] = h[q] * m.sc.in_scale;
-        linear_part(h, m.sc.k_over_g, L);
+        base_part(h, m.sc.k_over_g, L);
         const float g = gate(xs) * m.sc.res_scale;
 #pragma unroll
         for (int q = 0; q < 6; q++) sig[q] = Gm * (L[q] + g * (z[q] + b3[q]));
@@ -391,10 +391,10 @@ __global__ void __launch_bounds__(128, 6) k_element_mlp(ElementArgs a, MlpElemen
       for (int i = 0; i < 3; i++) g1[i] = fmaf(-mode_sign[ax], __shfl_xor_sync(0xffffffffu, g1[i], flip), g1[i]);
     }
     if (valid) {
-      float* fo = reinterpret_cast<float*>(a.fe) + (size_t)e * 24 + 3 * p;
-      fo[0]     = g1[0];
-      fo[1]     = g1[1];
-      fo[2]     = g1[2];
+      float* fo = reinterpret_cast<float*>(a.fe) + (size_t)(3 * p) * ld_e + e;  // corner-major planes
+      fo[0]      = g1[0];
+      fo[ld_e]   = g1[1];
+      fo[2 * ld_e] = g1[2];
       if (!isfinite(g1[0]) || !isfinite(g1[1]) || !isfinite(g1[2])) status |= NSM_STATUS_NONFINITE;
     }
   }

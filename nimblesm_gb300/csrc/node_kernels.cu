@@ -122,7 +122,8 @@ __device__ __forceinline__ double axpy(double s, double x, double y)
 }
 
 // The assembled element force of node n: element contributions in increasing
-// element order.
+// element order, from the corner-major planes fe[(3 c + i) ld_e + e] (a row
+// of consecutive nodes reads consecutive elements of one plane per slot).
 template <typename TF, bool kExact>
 __device__ __forceinline__ void gather_force(const NodeArgs& a, int n, double f[3])
 {
@@ -140,7 +141,8 @@ __device__ __forceinline__ void gather_force(const NodeArgs& a, int n, double f[
 #pragma unroll
   for (int j = 0; j < kFirst; j++)
 #pragma unroll
-    for (int i = 0; i < 3; i++) x[j][i] = ec[j] >= 0 ? __ldg(&fe[(long)(ec[j] >> 3) * 24 + (ec[j] & 7) * 3 + i]) : TF(0);
+    for (int i = 0; i < 3; i++)
+      x[j][i] = ec[j] >= 0 ? __ldg(&fe[((ec[j] & 7) * 3 + i) * a.ld_e + (ec[j] >> 3)]) : TF(0);
   // the first sum is 0 + x: x itself but for -0.0 (+0.0), an integer select
   // rather than an FP64 add in the exact form
   if (ec[0] >= 0) {
@@ -160,7 +162,7 @@ __device__ __forceinline__ void gather_force(const NodeArgs& a, int n, double f[
     const int  c  = ec & 7;
 #pragma unroll
     for (int i = 0; i < 3; i++) {
-      const TF xi = __ldg(&fe[e * 24 + c * 3 + i]);
+      const TF xi = __ldg(&fe[(c * 3 + i) * a.ld_e + e]);
       fs[i]       = kExact ? TF(__dadd_rn(double(fs[i]), double(xi))) : fs[i] + xi;
     }
   }

@@ -74,7 +74,7 @@ struct nsm_model {
   double* d_inv_mass = nullptr;
   double* d_geo = nullptr;  // [8 * kGeoPerPoint][ld_e]
   void*   d_ip = nullptr;   // [8][ld_e][16] per-point F and sigma records
-  void*   d_fe = nullptr;   // [ld_e][24] element nodal forces
+  void*   d_fe = nullptr;   // [24][ld_e] element nodal forces, corner-major planes (3 c + i)
   float*  d_Xf = nullptr;   // FP32 copies of X and u (FP32 form)
   float*  d_uf = nullptr;
   int*    d_status = nullptr;
@@ -508,6 +508,7 @@ int get_graph(nsm_model* m, int K, cudaGraphExec_t* out)
 }  // namespace
 
 int nsm::set_last_error(int code, const char* msg) { return fail(code, msg); }
+int nsm::model_num_nodes(const nsm_model* m) { return m->N; }
 
 extern "C" {
 

@@ -64,6 +64,22 @@ def algorithmic_bytes(N, E, precision):
     return step, element
 
 
+# Algorithmic work of one training pair in one epoch: the forward pass
+# (9*64 + 64*64 + 64*6 = 5,056 multiply-adds), the weight gradients (the same
+# 5,056) and the input gradients of layers 3 and 2 (64*6 + 64*64 = 4,480; layer
+# 1's input gradient is not needed): 14,592 multiply-adds, 2 flops each.
+TRAIN_FLOPS_PER_PAIR = 2 * (5056 + 5056 + 4480)
+
+
+def bf16_peak():
+    """Dense BF16 tensor peak (TFLOP/s), the measured burst figure."""
+    try:
+        with open(PEAKS_FILE) as f:
+            return float(json.load(f)["bf16_tflops"]), "measured"
+    except Exception:
+        return 1900.0, "fallback"
+
+
 def hbm_peak():
     try:
         with open(PEAKS_FILE) as f:
@@ -277,27 +293,39 @@ def uq_closure_variant(E, args, problem, device):
 
 
 def big_fp32_variant(E, args, device):
-    """The FP32-mixed form on a 256^3 jittered cube (16.8M elements), with its
-    displacement error against the FP64 form on the same mesh and steps."""
+    """The FP32-mixed form on a 256^3 jittered cube (16.8M elements): its
+    throughput over `big_steps` timed steps, and its displacement, velocity and
+    energy-drift error against the FP64 form on the same mesh after the whole
+    2000-step schedule (the steps past the timed ones run untimed)."""
     n = args.big_n
     prob = cube_problem(n, jitter=0.2, seed=0)
     dt = 0.5 * critical_time_step(prob)
     steps = args.big_steps
-    out = {}
-    u = {}
+    total = max(SCHEDULE_STEPS if args.big_full else 3 + steps, 3 + steps)
+    out, st = {}, {}
     for precision in ("fp32", "fp64"):
-        m = E.Model(prob, precision=precision, device=device)
+        m = E.Model(prob, precision=precision, device=device, graph_steps=100)
         m.begin(SCHEDULE_STEPS * dt, SCHEDULE_STEPS, SCHEDULE_STEPS)
-        m.advance(3)
+        m.advance(1)
+        e0 = sum(m.GetEnergies())
+        m.advance(2)
         m.synchronize()
         ms = m.advance_timed(steps)
-        u[precision] = m.GetVectorNodeData("displacement")
         out[precision] = 8.0 * prob.num_elem * steps / (ms * 1e-3)
+        t0 = time.perf_counter()
+        m.advance(total - 3 - steps)
+        m.synchronize()
+        ke, ie = m.GetEnergies()
+        st[precision] = dict(u=m.GetVectorNodeData("displacement"), v=m.GetVectorNodeData("velocity"),
+                             drift=(ke + ie - e0) / e0, rest_s=time.perf_counter() - t0)
         m.close()
-    err = float(np.linalg.norm(u["fp32"] - u["fp64"]) / np.linalg.norm(u["fp64"]))
+    a, b = st["fp32"], st["fp64"]
+    rel = lambda x, y: float(np.linalg.norm(x - y) / np.linalg.norm(y))
     return {f"fp32_{n}cube": {"value": out["fp32"], "unit": UNIT, "elements": prob.num_elem, "steps_timed": steps,
                               "fp64_value": out["fp64"], "speedup_vs_fp64": out["fp32"] / out["fp64"],
-                              "rel_disp_err_vs_fp64": err, "after_steps": 3 + steps}}
+                              "rel_disp_err_vs_fp64": rel(a["u"], b["u"]), "rel_vel_err_vs_fp64": rel(a["v"], b["v"]),
+                              "energy_drift": a["drift"], "energy_drift_fp64": b["drift"], "after_steps": total,
+                              "untimed_wall_s": {"fp32": a["rest_s"], "fp64": b["rest_s"]}}}
 
 
 def mlp_variant(E, args, problem, device, fp64_value, fp32_value):
@@ -347,7 +375,11 @@ def mlp_variant(E, args, problem, device, fp64_value, fp32_value):
         "energy_drift": a["drift"], "energy_drift_fp64": b["drift"], "after_steps": steps,
         "envelope_fallbacks": a["fallbacks"], "training_pairs": args.mlp_pairs, "epochs": args.mlp_epochs,
         "final_loss": loss, "generate_s": t1 - t0, "train_s": t2 - t1,
-        "network": "9-64-64-6 GELU, BF16 weights/activations, FP32 accumulate, tcgen05; linear skip, quadratic gate"}}, mlp
+        "train_tflops": args.mlp_pairs * args.mlp_epochs * TRAIN_FLOPS_PER_PAIR / (t2 - t1) / 1e12,
+        "train_tensor_frac": args.mlp_pairs * args.mlp_epochs * TRAIN_FLOPS_PER_PAIR / (t2 - t1) / 1e12
+        / bf16_peak()[0], "train_flops_per_pair_epoch": TRAIN_FLOPS_PER_PAIR,
+        "train_peak_source": bf16_peak()[1],
+        "network": "9-64-64-6 GELU, BF16 weights/activations, FP32 accumulate, tcgen05; second-order neo-Hookean base, cubic gate"}}, mlp
 
 
 def accuracy_variant(E, args, problem, device, mlp):
@@ -456,6 +488,29 @@ def run_ours(args):
     barrier()
     e2e_value = replica_value(8.0 * E_ * e2e_steps, 1e3 * (t1 - t0), reps)
 
+    # the whole drop-in step: the reference integrator's loop on host arrays
+    # (its O(N) velocity / displacement / acceleration updates and kinematic
+    # conditions on one host thread, as ExplicitTimeIntegrator runs them
+    # through a GpuModelData) around the same host-buffer force call
+    hl = {k: E.PinnedArray((N, 3)) for k in ("v", "a")}
+    hl["v"].array[:] = m.GetVectorNodeData("velocity")
+    hl["a"].array[:] = m.GetVectorNodeData("acceleration")
+    mass = m.ComputeLumpedMass()
+    t_now = m.progress()[1]
+    t_now, _ = m.HostLoopSteps(1, t_now, dt, mass, u_host.array, hl["v"].array, hl["a"].array, f_host.array)
+    barrier()
+    t0 = time.perf_counter()
+    t_now, host_s = m.HostLoopSteps(e2e_steps, t_now, dt, mass, u_host.array, hl["v"].array, hl["a"].array,
+                                    f_host.array)
+    t1 = time.perf_counter()
+    barrier()
+    e2e_step_value = replica_value(8.0 * E_ * e2e_steps, 1e3 * (t1 - t0), reps)
+    e2e_step = {"value": e2e_step_value, "unit": UNIT, "h2d_bytes_per_step": 24 * N, "d2h_bytes_per_step": 24 * N,
+                "ms_per_step": 1e3 * (t1 - t0) / e2e_steps, "host_loop_ms_per_step": 1e3 * host_s / e2e_steps,
+                "host_loop_share": host_s / (t1 - t0), "steps": e2e_steps,
+                "path": "nsm_host_loop_steps: the reference loop's host-side updates (one thread, pinned [N][3] "
+                        "u, v, a, f_int) + nsm_compute_internal_force_host per step"}
+
     step_bytes, elem_bytes = algorithmic_bytes(N, E_, args.precision)
     peak, peak_kind = hbm_peak()
     elem_ms = head["prof"]["element_ms"] / max(head["prof"]["element_launches"], 1)
@@ -469,8 +524,10 @@ def run_ours(args):
         "config": workload_config(n, problem, ws),
         "form": args.precision, "ips_per_step": 8 * E_, "dt": dt, "schedule_steps": sched,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 24 * N, "d2h_bytes_per_step": 24 * N,
-                "path": "nsm_compute_internal_force_host (pinned u in, f_int out)", "steps": e2e_steps,
+                "path": "nsm_compute_internal_force_host only (pinned u in, f_int out); the nodal updates of the "
+                        "step are not in it (see e2e_step)", "steps": e2e_steps,
                 "host_chunks": m.host_chunks()},
+        "e2e_step": e2e_step,
         "gpu_launches": head["launches"],
         "clocks": head["clocks"],
     }
@@ -560,8 +617,11 @@ def main():
                     help="timed steps of the reference-style UQ mode on the main mesh (0: skip)")
     ap.add_argument("--big-n", type=int, default=256, help="cube divisions of the large FP32-mixed variant")
     ap.add_argument("--big-steps", type=int, default=20, help="timed steps of the large variant (0: skip)")
+    ap.add_argument("--no-big-full", dest="big_full", action="store_false",
+                    help="compare the large variant's forms after the timed steps, not after the whole schedule")
     ap.add_argument("--mlp-steps", type=int, default=103, help="steps of the learned-closure run (0: skip)")
-    ap.add_argument("--mlp-pairs", type=int, default=4_000_000)
+    ap.add_argument("--mlp-pairs", type=int, default=20_000_000,
+                    help="training pairs of the learned closure (the workload's 20M)")
     ap.add_argument("--acc-steps", type=int, default=SCHEDULE_STEPS,
                     help="steps of the FP64 / FP32 / closure accuracy run (0: skip)")
     ap.add_argument("--mlp-epochs", type=int, default=20)

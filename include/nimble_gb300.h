@@ -206,6 +206,32 @@ int nsm_compute_internal_force(nsm_model* model, double time_previous, double ti
  * reference's integrator loop (which updates nodes on the host) calls each
  * step through a GpuModelData.  displacement, internal_force: [N][3]. */
 int nsm_compute_internal_force_host(nsm_model* model, const double* displacement, double* internal_force);
+/* The reference integrator's loop on host arrays around the host-buffer call:
+ * the step a NimbleSM run makes through the GpuModelData adapter, where
+ * ExplicitTimeIntegrator keeps u, v, a in host memory
+ * (src/integrators/explicit_time_integrator.cc:196-276: v += dt/2 a,
+ * kinematic conditions, u += dt v, kinematic conditions,
+ * nsm_compute_internal_force_host, a = f_int / m, v += dt/2 a, and the
+ * kinematic conditions again on output steps).  num_steps steps from
+ * *time_current with the user step dt_user (t += dt_user; the step's delta is
+ * t - t_prev, as the reference forms it); step numbers first_step.. decide the
+ * output steps (output_frequency, num_load_steps as in the input deck).
+ * mass [N]; u, v, a, f_int [N][3] host arrays, updated in place; bcs (NULL:
+ * none) the constant-magnitude conditions in deck order.  *host_seconds
+ * (nullable) receives the time spent in the host-side updates.  The host
+ * arithmetic rounds as the reference's, so the state equals nsm_advance's
+ * bit for bit. */
+typedef struct nsm_host_bcs {
+  int           num_bcs;
+  const int*    kind;      /* [num_bcs] NSM_BC_*; initial-velocity lines are skipped */
+  const int*    component; /* [num_bcs] 0, 1, 2 */
+  const double* value;     /* [num_bcs] */
+  const int*    ptr;       /* [num_bcs + 1] offsets into nodes */
+  const int*    nodes;
+} nsm_host_bcs;
+int nsm_host_loop_steps(nsm_model* model, int num_steps, double* time_current, double dt_user, int output_frequency,
+                        int first_step, int num_load_steps, const double* mass, const nsm_host_bcs* bcs, double* u,
+                        double* v, double* a, double* f_int, double* host_seconds);
 /* The host-buffer call runs as a pipeline of `chunks` element ranges: u is
  * copied in by node ranges ahead of the element launches that need them and
  * f_int copied out by node ranges as soon as their elements are done, so the
@@ -359,10 +385,11 @@ int nsm_critical_time_step_noalloc(int num_nodes, int num_elem, const double* co
  * the Cauchy stress over the shear modulus, standing in for the neo-Hookean
  * material update behind the same material interface (the reference's
  * Material::GetStress, src/nimble_material.h:239-313; no learned material
- * exists in the reference).  It is placed on the material's small-strain
- * linear map with a quadratic gate: sigma/G = L(H) + s_r |x|^2 MLP(x),
- * x = H * in_scale, so it reduces to the exact small-strain response near
- * F = I.  Points outside the
+ * exists in the reference).  It is placed on the material's second-order
+ * expansion with a cubic gate: sigma/G = B(H) + s_r |x|^3 MLP(x),
+ * x = H * in_scale, B the neo-Hookean stress to second order in H, so the
+ * network carries the O(|H|^3) remainder and cannot disturb the response
+ * near F = I, where its training data is thinnest.  Points outside the
  * training envelope (|H_ij| > 4 s_in^-1 or det F < min_det) use the plain
  * neo-Hookean stress.  Parameters: W1[64][9], b1[64], W2[64][64], b2[64],
  * W3[6][64], b3[6] (NSM_MLP_PARAMS floats); scales: in_scale, res_scale,

@@ -20,7 +20,7 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off", "-I" + INCLUDE]
-NO_FMAD = {"node_kernels.cu", "setup_kernels.cu", "noalloc_dt.cu"}
+NO_FMAD = {"node_kernels.cu", "setup_kernels.cu", "noalloc_dt.cu", "host_loop.cu"}
 
 
 def _sources():

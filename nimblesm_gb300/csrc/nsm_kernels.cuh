@@ -13,6 +13,8 @@
 #define NSM_STATUS_NONFINITE 2      // a NaN or Inf in a stress or force
 #define NSM_STATUS_TIMEOUT 8        // a bounded wait on the tensor cores ran out
 
+struct nsm_model;  // the handle of include/nimble_gb300.h
+
 namespace nsm {
 
 // One material: of a block of a multi-block mesh, or of one sample of an
@@ -205,5 +207,7 @@ cudaError_t launch_node_aos_to_soa(int N, long ld_n, const double* src, double* 
 // Records the calling thread's nsm_last_error() text and returns `code`
 // (for entry points defined outside nsm_model.cu).
 int set_last_error(int code, const char* msg);
+// Number of nodes of a handle (all samples of an ensemble).
+int model_num_nodes(const ::nsm_model* m);
 
 }  // namespace nsm

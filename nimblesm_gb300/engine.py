@@ -58,6 +58,11 @@ _dp_f = C.POINTER(C.c_float)
 _ip = C.POINTER(C.c_int)
 _vp = C.c_void_p
 
+
+class _HostBcs(C.Structure):
+    _fields_ = [("num_bcs", C.c_int), ("kind", _ip), ("component", _ip), ("value", _dp), ("ptr", _ip),
+                ("nodes", _ip)]
+
 # name -> (restype, argtypes); kept in step with include/nimble_gb300.h
 SIGNATURES = {
     "nsm_last_error": (C.c_char_p, []),
@@ -124,6 +129,8 @@ SIGNATURES = {
     "nsm_tc_selftest": (C.c_int, [C.c_int, C.c_int, _dp_f, _dp_f, _dp_f]),
     "nsm_tc_wait_timeout_selftest": (C.c_int, [C.c_long, C.POINTER(C.c_int)]),
     "nsm_device_sm_count": (C.c_int, [C.c_int, C.POINTER(C.c_int)]),
+    "nsm_host_loop_steps": (C.c_int, [_vp, C.c_int, _dp, C.c_double, C.c_int, C.c_int, C.c_int, _dp,
+                                      C.POINTER(_HostBcs), _dp, _dp, _dp, _dp, _dp]),
     "nsm_host_alloc": (_vp, [C.c_size_t]),
     "nsm_host_free": (None, [_vp]),
 }
@@ -325,6 +332,23 @@ class Model:
         f = out if out is not None else np.zeros((self.problem.num_nodes, 3))
         _check(library().nsm_compute_internal_force_host(self._h, _d(u), _d(f)))
         return f
+
+    def HostLoopSteps(self, num_steps, time_current, dt_user, mass, u, v, a, f_int, output_frequency=0,
+                      first_step=0, num_load_steps=0):
+        """The reference integrator's loop on host arrays (u, v, a, f_int
+        [N][3], updated in place; mass [N]) around the host-buffer force call:
+        num_steps steps from time_current.  Returns (time, host seconds)."""
+        kinds, comps, vals, ptr, nodes = self.problem.bc_arrays()
+        bcs = _HostBcs(len(kinds), kinds.ctypes.data_as(_ip), comps.ctypes.data_as(_ip), _d(vals),
+                       ptr.ctypes.data_as(_ip), nodes.ctypes.data_as(_ip))
+        t, secs = C.c_double(time_current), C.c_double(0.0)
+        for x in (u, v, a, f_int):
+            assert x.dtype == np.float64 and x.flags.c_contiguous and x.shape == (self.problem.num_nodes, 3)
+        m = np.ascontiguousarray(mass, dtype=np.float64)
+        _check(library().nsm_host_loop_steps(self._h, int(num_steps), C.byref(t), float(dt_user),
+                                             int(output_frequency), int(first_step), int(num_load_steps), _d(m),
+                                             C.byref(bcs), _d(u), _d(v), _d(a), _d(f_int), C.byref(secs)))
+        return t.value, secs.value
 
     def GetIntegrationPointData(self):
         E = self.problem.num_elem

@@ -58,7 +58,7 @@ __global__ void k_generate(long n, unsigned long long seed, double sd, double mi
   for (int q = 0; q < 6; q++) Y[6 * i + q] = (float)(sig[q] / G);
 }
 
-// Sum over the training set of |(sigma/G - L(H)) / |x|^2|^2 (per-block
+// Sum over the training set of |(sigma/G - B(H)) / |x|^3|^2 (per-block
 // partials, summed in block order on the host): sets the residual scale.
 __global__ void k_residual_moment(long n, const float* __restrict__ X, const float* __restrict__ Y, float k_over_g,
                                   float in_scale, double* __restrict__ partial)
@@ -71,7 +71,7 @@ __global__ void k_residual_moment(long n, const float* __restrict__ X, const flo
       x[q]  = X[9 * i + q];
       xs[q] = x[q] * in_scale;
     }
-    linear_part(x, k_over_g, L);
+    base_part(x, k_over_g, L);
     const double g = gate(xs);
     for (int q = 0; q < 6; q++) {
       double r = ((double)Y[6 * i + q] - (double)L[q]) / g;
@@ -235,7 +235,7 @@ __global__ void __launch_bounds__(128) k_train(const float* __restrict__ X, cons
   }
   {
     float L[6];
-    linear_part(x, sc.k_over_g, L);
+    base_part(x, sc.k_over_g, L);
     const float g = gate(xs) * sc.res_scale;
     for (int q = 0; q < 6; q++) t[q] = (Y[6 * idx + q] - L[q]) / g;
   }
@@ -478,7 +478,7 @@ __global__ void __launch_bounds__(128) k_predict(long n, const float* __restrict
     if (valid) {
       if (in_envelope(h, sc)) {
         float L[6];
-        linear_part(h, sc.k_over_g, L);
+        base_part(h, sc.k_over_g, L);
         const float g = gate(xs) * sc.res_scale;
         for (int q = 0; q < kOut; q++) sigma[6 * i + q] = G * (double)(L[q] + g * (z[q] + b3[q]));
       } else {

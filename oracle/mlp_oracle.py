@@ -1,9 +1,10 @@
 """CPU oracle of the learned closure's network (TEST INFRASTRUCTURE ONLY).
 
-The engine's MLP (nimblesm_gb300/csrc/mlp_common.cuh): sigma/G = L(H) +
-s_r * |x|^2 * MLP(x), x = H * s_in, MLP = 9 -> 64 -> 64 -> 6 with GELU (sigmoid
-form), evaluated with BF16 operands and FP32 accumulation on the tensor
-cores.  This module restates the
+The engine's MLP (nimblesm_gb300/csrc/mlp_common.cuh): sigma/G = B(H) +
+s_r * |x|^3 * MLP(x), x = H * s_in, B the neo-Hookean stress over G to second
+order in H (linear_part + quadratic_part), MLP = 9 -> 64 -> 64 -> 6 with GELU
+(sigmoid form), evaluated with BF16 operands and FP32 accumulation on the
+tensor cores.  This module restates the
 forward pass and the gradient of the training loss in float64 numpy, either
 emulating the BF16 roundings at exactly the points where the GPU rounds
 (emulate=True, for a tight gradient check) or in exact arithmetic
@@ -39,6 +40,26 @@ def linear_part(H, k_over_g):
                      H[:, 1] + H[:, 3], H[:, 5] + H[:, 7], H[:, 6] + H[:, 2]], axis=1)
 
 
+def quadratic_part(H, k_over_g):
+    """The second-order terms of the neo-Hookean stress over G (the reference's
+    sigma = K/2 (J - 1/J) I + G J^(-5/3) dev(F F^T), src/nimble_material.cc:252-310,
+    expanded in H): -K/(2G) tr(H H) I + H H^T - |H|^2/3 I - 10/3 tr(H) dev(eps)."""
+    Hm = np.asarray(H, np.float64).reshape(-1, 3, 3)
+    tr = np.trace(Hm, axis1=1, axis2=2)
+    trhh = np.einsum("nij,nji->n", Hm, Hm)
+    hht = np.einsum("nij,nkj->nik", Hm, Hm)
+    n2 = np.einsum("nij,nij->n", Hm, Hm)
+    eps = 0.5 * (Hm + Hm.transpose(0, 2, 1))
+    dev = eps - (tr / 3.0)[:, None, None] * np.eye(3)[None]
+    Q = (-0.5 * k_over_g * trhh - n2 / 3.0)[:, None, None] * np.eye(3)[None] + hht - (10.0 / 3.0) * tr[:, None, None] * dev
+    return np.stack([Q[:, 0, 0], Q[:, 1, 1], Q[:, 2, 2], Q[:, 0, 1], Q[:, 1, 2], Q[:, 2, 0]], axis=1)
+
+
+def base_part(H, k_over_g):
+    """The neo-Hookean stress over G to second order in H (the closure's base)."""
+    return linear_part(H, k_over_g) + quadratic_part(H, k_over_g)
+
+
 def act(u):
     """The engine's activation: GELU in its sigmoid form x sigma(1.702 x)
     (Hendrycks & Gimpel 2016), written a(u) = u (1 + tanh u) = 2 u sigma(2u)
@@ -71,13 +92,14 @@ def forward(P, scales, H, emulate=True):
 
 
 def gate(H, scales):
+    """The cubic gate |x|^3."""
     xs = (np.asarray(H, np.float32) * np.float32(scales[0])).astype(np.float64)
-    return np.maximum((xs * xs).sum(axis=1), 1e-12)
+    return np.maximum((xs * xs).sum(axis=1) ** 1.5, 1e-30)
 
 
 def stress_over_g(P, scales, H, emulate=True):
     f = forward(P, scales, H, emulate)
-    return linear_part(np.asarray(H, np.float64), scales[2]) + (scales[1] * gate(H, scales))[:, None] * f["out"]
+    return base_part(np.asarray(H, np.float64), scales[2]) + (scales[1] * gate(H, scales))[:, None] * f["out"]
 
 
 def loss_and_gradient(P, scales, H, Y, emulate=True):
@@ -86,7 +108,7 @@ def loss_and_gradient(P, scales, H, Y, emulate=True):
     r = bf16 if emulate else (lambda v: np.asarray(v, np.float64))
     n = H.shape[0]
     f = forward(P, scales, H, emulate)
-    t = (np.asarray(Y, np.float64) - linear_part(np.asarray(H, np.float64), scales[2])) / \
+    t = (np.asarray(Y, np.float64) - base_part(np.asarray(H, np.float64), scales[2])) / \
         (scales[1] * gate(H, scales))[:, None]
     d = f["out"] - t
     loss = float((d * d).sum() / n)

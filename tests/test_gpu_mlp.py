@@ -69,7 +69,11 @@ def test_gradient_matches_oracle(mlp):
         assert rel(g[lo:hi], g_e[lo:hi]) < 3e-2
 
 
-def test_training_gains_over_the_linear_part(mlp):
+def test_training_gains_over_the_analytic_base(mlp):
+    """What the trained network adds: on the training distribution its stress
+    is closer to the material's than the analytic base alone (the stress to
+    second order in H, with the network's term left out), and far closer than
+    the small-strain linear part."""
     mlp.set_params(E.MLPClosure(K, G, seed=3).params()[0])  # fresh weights, keep the data's scales
     loss = mlp.train(epochs=40, batch_tiles=16, lr=5e-3)
     P, S = mlp.params()
@@ -79,12 +83,16 @@ def test_training_gains_over_the_linear_part(mlp):
     exact = O.stress(F, K, G) / G
     sig, fb = mlp.predict(F)
     inside = np.abs(H).max(axis=1) <= S[3]
+    base = M.base_part(H, S[2])
     lin = M.linear_part(H, S[2])
     e_mlp = rel(sig[inside] / G, exact[inside])
+    e_base = rel(base[inside], exact[inside])
     e_lin = rel(lin[inside], exact[inside])
-    print(f"loss {loss:.3e}  stress error: linear part {e_lin:.3e}, with the trained network {e_mlp:.3e}")
+    print(f"loss {loss:.3e}  stress error: linear part {e_lin:.3e}, second-order base {e_base:.3e}, "
+          f"with the trained network {e_mlp:.3e}")
     assert loss < 0.05
-    assert e_mlp < 0.05 * e_lin, (e_mlp, e_lin)
+    assert e_mlp < 0.25 * e_base, (e_mlp, e_base)
+    assert e_mlp < 0.02 * e_lin, (e_mlp, e_lin)
 
 
 def test_fused_element_kernel_matches_predict(mlp):
@@ -132,17 +140,19 @@ def test_fused_forces_match_the_material(mlp):
 
 
 def test_small_strain_limit(mlp):
-    """The gated closure reduces to the material's small-strain response: at
-    strains of 1e-4 its stress error is far below the linear part's own
-    O(|H|) model error of the neo-Hookean material, not a network error floor."""
+    """The gated closure reduces to the material's response near F = I: at
+    strains of 1e-4 and 1e-3 its stress error is the FP32 evaluation's and the
+    third-order remainder's, far below the second-order terms (1e-4 and 1e-3
+    of the stress) that a network error near H = 0 would disturb."""
     P, S = mlp.params()
     rng = np.random.default_rng(7)
-    H = rng.normal(0, 1e-4, size=(2048, 9))
-    F = to_reference_F(H)
-    exact = O.stress(F, K, G) / G
-    sig, fb = mlp.predict(F)
-    assert fb == 0
-    assert rel(sig / G, exact) < 1e-3
+    for scale in (1e-4, 1e-3):
+        H = rng.normal(0, scale, size=(2048, 9))
+        F = to_reference_F(H)
+        exact = O.stress(F, K, G) / G
+        sig, fb = mlp.predict(F)
+        assert fb == 0
+        assert rel(sig / G, exact) < 2e-5, (scale, rel(sig / G, exact))
 
 
 def test_explicit_run_with_the_closure(mlp):
@@ -162,3 +172,38 @@ def test_explicit_run_with_the_closure(mlp):
     print(f"closure run: relative displacement error {e:.3e} after {steps} steps, fallbacks {m.closure_fallbacks()}")
     assert e < 1e-3
     assert m.closure_fallbacks() == 0
+
+
+def test_closure_over_the_full_schedule():
+    """The workload's whole schedule (2000 steps at dt = 0.5 dt_crit) with the
+    closure as the material, trained as the benchmark trains it (20M pairs of
+    the material, 20 epochs), on a 32^3 jittered cube: displacement within
+    1e-3 of the FP64 plain run after the last step; the energy drift of both
+    runs is reported.  (At 32^3 the schedule covers 4x the physical time of
+    the 128^3 one, dt being proportional to the element size.)"""
+    from nimblesm_gb300.mesh import cube_problem, critical_time_step
+    p = cube_problem(32, jitter=0.2, seed=0)
+    mlp = E.MLPClosure(p.bulk_modulus, p.shear_modulus, seed=1)
+    mlp.generate(20_000_000, seed=7, perturbation=0.05, min_det=0.5)
+    loss = mlp.train(epochs=20, batch_tiles=16, lr=5e-3)
+    dt = 0.5 * critical_time_step(p)
+    steps = 2000
+    out = {}
+    for form in ("fp64", "mlp"):
+        m = E.Model(p, precision="fp64" if form == "fp64" else "fp32", graph_steps=100)
+        if form == "mlp":
+            m.set_closure(mlp)
+        m.begin(steps * dt, steps, 0)
+        m.advance(1)
+        e0 = sum(m.GetEnergies())
+        m.advance(steps - 1)
+        st = m.state(with_ip=False)
+        out[form] = (st, (sum(m.GetEnergies()) - e0) / e0, m.closure_fallbacks() if form == "mlp" else 0)
+        m.close()
+    mlp.close()
+    (ref, drift64, _), (st, drift, fallbacks) = out["fp64"], out["mlp"]
+    e_u, e_v = rel(st["u"], ref["u"]), rel(st["v"], ref["v"])
+    print(f"closure (loss {loss:.2e}), 32^3 x {steps} steps: displacement error {e_u:.3e}, velocity error {e_v:.3e}, "
+          f"energy drift {drift:.3e} (FP64 plain {drift64:.3e}), fallbacks {fallbacks}")
+    assert e_u < 1e-3
+    assert abs(drift) < 1e-2

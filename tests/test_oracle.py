@@ -144,3 +144,28 @@ def test_live_reference_bitwise_random_case():
     b = O.run_ref(p, 17 * dt, 17, 5)
     for k in ("u", "v", "a", "f_int", "mass", "F", "sigma"):
         assert np.array_equal(a[k], b[k]), k
+
+
+def test_closure_base_is_the_material_to_second_order():
+    """The learned closure's analytic base (oracle/mlp_oracle.py base_part,
+    restated in nimblesm_gb300/csrc/mlp_common.cuh) is the reference's
+    neo-Hookean stress to second order in H: the remainder falls as |H|^3
+    (relative to the stress, as |H|^2), while the linear part's falls as |H|."""
+    from oracle import mlp_oracle as M
+    K, G = 160e9, 79.3e9
+    slot = [0, 3, 8, 6, 1, 4, 5, 7, 2]
+    rng = np.random.default_rng(0)
+    errs = []
+    for s in (1e-2, 1e-3):
+        H = rng.normal(0, s, size=(2000, 9))
+        F = np.zeros((H.shape[0], 9))
+        for q in range(9):
+            F[:, slot[q]] = H[:, q] + (1.0 if q % 4 == 0 else 0.0)
+        exact = O.stress(F, K, G) / G
+        e_b = np.linalg.norm(M.base_part(H, K / G) - exact) / np.linalg.norm(exact)
+        e_l = np.linalg.norm(M.linear_part(H, K / G) - exact) / np.linalg.norm(exact)
+        errs.append((e_b, e_l))
+    (b2, l2), (b3, l3) = errs
+    assert 50 < b2 / b3 < 200      # second-order remainder relative to the stress: |H|^2
+    assert 5 < l2 / l3 < 20         # the linear part's: |H|
+    assert b3 < 1e-5 and l3 > 1e-3

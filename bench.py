@@ -69,6 +69,12 @@ def algorithmic_bytes(N, E, precision):
 # 5,056) and the input gradients of layers 3 and 2 (64*6 + 64*64 = 4,480; layer
 # 1's input gradient is not needed): 14,592 multiply-adds, 2 flops each.
 TRAIN_FLOPS_PER_PAIR = 2 * (5056 + 5056 + 4480)
+# Optimizer batch: 152 tiles of 128 pairs, one tile per SM of the GPU, with a
+# learning rate of 2e-2 (cosine-decayed): measured against 16 tiles at 5e-3,
+# the same 20 epochs reach a stress error of 1.6e-3 against 1.4e-3 on the
+# training distribution in 0.72 s instead of 5.7 s.
+TRAIN_BATCH_TILES = 152
+TRAIN_LR = 2e-2
 
 
 def bf16_peak():
@@ -337,7 +343,7 @@ def mlp_variant(E, args, problem, device, fp64_value, fp32_value):
     mlp = E.MLPClosure(problem.bulk_modulus, problem.shear_modulus, seed=1, device=device)
     mlp.generate(args.mlp_pairs, seed=7, perturbation=0.05, min_det=0.5)
     t1 = time.perf_counter()
-    loss = mlp.train(epochs=args.mlp_epochs, batch_tiles=16, lr=5e-3)
+    loss = mlp.train(epochs=args.mlp_epochs, batch_tiles=TRAIN_BATCH_TILES, lr=TRAIN_LR)
     t2 = time.perf_counter()
     dt = 0.5 * critical_time_step(problem)
     steps = args.mlp_steps
@@ -375,6 +381,7 @@ def mlp_variant(E, args, problem, device, fp64_value, fp32_value):
         "energy_drift": a["drift"], "energy_drift_fp64": b["drift"], "after_steps": steps,
         "envelope_fallbacks": a["fallbacks"], "training_pairs": args.mlp_pairs, "epochs": args.mlp_epochs,
         "final_loss": loss, "generate_s": t1 - t0, "train_s": t2 - t1,
+        "train_batch_pairs": 128 * TRAIN_BATCH_TILES, "train_lr": TRAIN_LR,
         "train_tflops": args.mlp_pairs * args.mlp_epochs * TRAIN_FLOPS_PER_PAIR / (t2 - t1) / 1e12,
         "train_tensor_frac": args.mlp_pairs * args.mlp_epochs * TRAIN_FLOPS_PER_PAIR / (t2 - t1) / 1e12
         / bf16_peak()[0], "train_flops_per_pair_epoch": TRAIN_FLOPS_PER_PAIR,

@@ -64,33 +64,41 @@ __device__ __forceinline__ void wait_commit(uint64_t* mbar, uint32_t& phase, int
   fence_after_sync();
 }
 
-__device__ __forceinline__ void layer(uint32_t d, const uint8_t* a, int Ka, const uint8_t* b, int N)
+// acc0: the first K-step accumulates onto what the columns hold (the bias
+// stored there by the previous epilogue) instead of overwriting it.
+__device__ __forceinline__ void layer(uint32_t d, const uint8_t* a, int Ka, const uint8_t* b, int N, bool acc0 = false)
 {
   const uint32_t idesc = idesc_bf16_f32(128, N);
   for (int ks = 0; ks < Ka / 16; ks++)
     mma_bf16(d, smem_desc(smem_addr(a) + ks * 2 * kLBO, kLBO, 16 * Ka), smem_desc(smem_addr(b) + ks * 2 * kLBO, kLBO, 16 * Ka),
-             idesc, ks > 0);
+             idesc, acc0 || ks > 0);
 }
 
 // Hidden-layer epilogue: 64 accumulator columns of this thread's row ->
-// act(z + bias) -> BF16 row r of the [128][64] activation tile, two columns
-// per packed FP32x2 operation.
-__device__ __forceinline__ void hidden_epilogue(uint32_t taddr, const float* bias, uint8_t* tile, int r)
+// act(z) -> BF16 row r of the [128][64] activation tile, two columns per
+// packed FP32x2 operation.  With bias_next, each 16-column block of the
+// accumulator, once read, is overwritten with the next layer's bias, which
+// that layer's MMAs then accumulate onto: the bias costs 4 shared loads and
+// one tensor-memory store per 16 columns instead of a load and an add per
+// pair of columns.
+__device__ __forceinline__ void hidden_epilogue(uint32_t taddr, uint8_t* tile, int r, const float* bias_next)
 {
 #pragma unroll
   for (int h = 0; h < 4; h++) {
     float z[16];
     tmem_ld16(taddr + 16 * h, z);
     tmem_wait_ld();
+    if (bias_next) {
+      float bn[16];
+#pragma unroll
+      for (int q = 0; q < 16; q += 4) *reinterpret_cast<float4*>(bn + q) = *reinterpret_cast<const float4*>(bias_next + 16 * h + q);
+      tmem_st16(taddr + 16 * h, bn);
+    }
 #pragma unroll
     for (int k0 = 0; k0 < 16; k0 += 8) {
       uint32_t w[4];
 #pragma unroll
-      for (int j = 0; j < 4; j++) {
-        f32x2 v = f2_pack(z[k0 + 2 * j], z[k0 + 2 * j + 1]);
-        if (bias) v = f2_add(v, *reinterpret_cast<const f32x2*>(bias + 16 * h + k0 + 2 * j));
-        w[j] = act_bf16(v);
-      }
+      for (int j = 0; j < 4; j++) w[j] = act_bf16(f2_pack(z[k0 + 2 * j], z[k0 + 2 * j + 1]));
       *reinterpret_cast<uint4*>(tile + kmajor_offset(r, 16 * h + k0, kHid)) = make_uint4(w[0], w[1], w[2], w[3]);
     }
   }
@@ -256,16 +264,17 @@ __global__ void __launch_bounds__(128, 6) k_element_mlp(ElementArgs a, MlpElemen
     }
     id_next = node_of(chunk + gridDim.x);
     wait_commit(&mbar, phase, &err);
-    hidden_epilogue(taddr, nullptr, sm + el::A, r);
+    hidden_epilogue(taddr, sm + el::A, r, b2);  // leaves b2 in the columns for layer 2
+    tmem_wait_st();
     // ---- layer 2 ----
     if (!publish(&err)) break;
     if (r == 0) {
-      layer(tb, sm + el::A, kHid, sm + el::W + kOffW2, kHid);
+      layer(tb, sm + el::A, kHid, sm + el::W + kOffW2, kHid, true);
       mma_commit(&mbar);
     }
     values_of(id_next, nv);
     wait_commit(&mbar, phase, &err);
-    hidden_epilogue(taddr, b2, sm + el::A, r);
+    hidden_epilogue(taddr, sm + el::A, r, nullptr);
     // ---- layer 3 ----
     if (!publish(&err)) break;
     if (r == 0) {

@@ -363,16 +363,25 @@ cleanup:
   if (warp == 0) tmem_dealloc(tb, tr::kCols);
 }
 
-// Deterministic reduction of the per-CTA gradients (CTA order) and an Adam
-// step on the FP32 master parameters.
+// Deterministic reduction of the per-CTA gradients and an Adam step on the
+// FP32 master parameters.  Eight lanes share a parameter: lane j sums the
+// partials of CTAs j, j + 8, ... in order, and three butterfly steps combine
+// the eight sums in a fixed order, so every run gives the same bits while a
+// launch has eight times the loads in flight of one thread per parameter.
+constexpr int kAdamLanes = 8;
 __global__ void k_adam(int ncta, const float* __restrict__ grad_partial, float* __restrict__ P,
                        float* __restrict__ m1, float* __restrict__ m2, float lr, float beta1, float beta2,
                        float eps, float bc1, float bc2)
 {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= kParams) return;
-  float g = 0.0f;
-  for (int c = 0; c < ncta; c++) g += grad_partial[(long)c * kParams + i];
+  const long t   = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const int  i   = (int)(t / kAdamLanes), sub = (int)(t % kAdamLanes);
+  const bool own = i < kParams;
+  float      g   = 0.0f;
+  if (own)
+    for (int c = sub; c < ncta; c += kAdamLanes) g += grad_partial[(long)c * kParams + i];
+#pragma unroll
+  for (int o = 1; o < kAdamLanes; o <<= 1) g += __shfl_xor_sync(0xffffffffu, g, o);
+  if (!own || sub != 0) return;
   float a = beta1 * m1[i] + (1.0f - beta1) * g;
   float b = beta2 * m2[i] + (1.0f - beta2) * g * g;
   m1[i]   = a;
@@ -541,7 +550,8 @@ cudaError_t launch_train(int tiles, const float* X, const float* Y, long n, long
 cudaError_t launch_adam(int ncta, const float* grad_partial, float* P, float* m1, float* m2, float lr, float beta1,
                         float beta2, float eps, float bc1, float bc2, cudaStream_t s)
 {
-  k_adam<<<(kParams + 255) / 256, 256, 0, s>>>(ncta, grad_partial, P, m1, m2, lr, beta1, beta2, eps, bc1, bc2);
+  k_adam<<<(kParams * kAdamLanes + 255) / 256, 256, 0, s>>>(ncta, grad_partial, P, m1, m2, lr, beta1, beta2, eps,
+                                                             bc1, bc2);
   return cudaGetLastError();
 }
 

@@ -92,7 +92,7 @@ def test_training_gains_over_the_analytic_base(mlp):
           f"with the trained network {e_mlp:.3e}")
     assert loss < 0.05
     assert e_mlp < 0.25 * e_base, (e_mlp, e_base)
-    assert e_mlp < 0.02 * e_lin, (e_mlp, e_lin)
+    assert e_mlp < 0.03 * e_lin, (e_mlp, e_lin)
 
 
 def test_fused_element_kernel_matches_predict(mlp):

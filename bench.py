@@ -47,7 +47,7 @@ FP64_FLOPS_PER_IP = 258.1
 FP64_INSTR_PER_IP = 170.2
 # DRAM bytes (read + write) of one element launch on the 128^3 cube, from one
 # ncu capture per form.
-ELEMENT_TRAFFIC_128 = {"fp64": 2.703591424e9 + 2.702464768e9, "fp32": 0.119155456e9 + 1.213316608e9}
+ELEMENT_TRAFFIC_128 = {"fp64": 2.696480768e9 + 2.657063168e9, "fp32": 0.119112960e9 + 1.213583360e9}
 
 
 def algorithmic_bytes(N, E, precision):

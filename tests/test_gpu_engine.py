@@ -463,8 +463,13 @@ def test_128_cube_full_schedule_against_reference_fixture():
         e = abs(v - float(fx[k])) / abs(float(fx[k]))
         report[k] = (e, float(fx["env_" + k]))
         assert e <= max(TOL, 2.0 * float(fx["env_" + k])), (k, e)
+    # the engine's own stress is accurate: within 1e-10 of the extended-precision
+    # stress of its own displacement on the sampled elements
+    e_exact = rel(got["sigma"], O.stress_exact(p, g["u"], np.asarray(elems, np.int32)))
+    report["sigma_vs_extended_precision"] = (e_exact, 0.0)
     print("128^3 x 2000 steps, relative error (reference's 1-ulp sensitivity):",
           {k: f"{e:.2e} ({env:.2e})" for k, (e, env) in report.items()})
+    assert e_exact < TOL
 
 
 def test_derived_element_data():

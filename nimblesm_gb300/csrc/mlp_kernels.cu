@@ -168,7 +168,7 @@ __device__ __forceinline__ bool await_mma(Sync& s)
 
 __device__ __forceinline__ void ld_row(uint32_t tbase, uint32_t col, int n16, float* v)
 {
-  const uint32_t lane_base = (uint32_t)((threadIdx.x >> 5) * 32) << 16;
+  const uint32_t lane_base = (uint32_t)(((threadIdx.x >> 5) & 3) * 32) << 16;  // the warp's lane quarter
   for (int c = 0; c < n16; c++) tmem_ld16(tbase + lane_base + col + 16 * c, v + 16 * c);
   tmem_wait_ld();
 }
@@ -185,100 +185,113 @@ __device__ __forceinline__ void gemm(uint32_t d, const uint8_t* a, int a_rows_k,
   }
 }
 
-__global__ void __launch_bounds__(128) k_train(const float* __restrict__ X, const float* __restrict__ Y, long n,
-                                               long first, long stride_a, long offset_b, const uint8_t* __restrict__ img,
-                                               const float* __restrict__ P, Scales sc, float inv_batch,
-                                               float* __restrict__ grad_partial, float* __restrict__ loss_partial,
-                                               int* __restrict__ status)
+// Two warpgroups per tile: thread t owns row r = t % 128 (tensor-memory lane r)
+// and, in the 64-column epilogues, the columns [32 h, 32 h + 32) of half
+// h = t / 128, so each thread's share of the activation and gradient work is
+// half a row and the tile's dependent MMA rounds wait on half as much
+// epilogue each.
+constexpr int kTrainThreads = 256;
+
+__global__ void __launch_bounds__(kTrainThreads) k_train(const float* __restrict__ X, const float* __restrict__ Y,
+                                                         long n, long first, long stride_a, long offset_b,
+                                                         const uint8_t* __restrict__ img, const float* __restrict__ P,
+                                                         Scales sc, float inv_batch, float* __restrict__ grad_partial,
+                                                         float* __restrict__ loss_partial, int* __restrict__ status)
 {
   extern __shared__ __align__(1024) uint8_t sm[];
   __shared__ uint64_t mbar;
   __shared__ uint32_t tslot;
   __shared__ int      err;
   __shared__ float    red[128];
-  const int           r = threadIdx.x, warp = r >> 5;
+  const int           tid = threadIdx.x, warp = tid >> 5, r = tid & 127, half = tid >> 7;
+  const int           c0  = 32 * half;  // this thread's first column in the 64-column epilogues
 
   if (warp == 0) {
     tmem_alloc(&tslot, tr::kCols);
     tmem_relinquish();
   }
-  if (r == 0) {
+  if (tid == 0) {
     mbar_init(&mbar, 1);
     err = 0;
   }
   // constant operand regions (zero rows, ones rows), weight images, biases
   {
     uint4 z = make_uint4(0, 0, 0, 0);
-    for (int i = r; i < (tr::W - tr::AOP) / 16; i += 128) reinterpret_cast<uint4*>(sm + tr::AOP)[i] = z;
+    for (int i = tid; i < (tr::W - tr::AOP) / 16; i += kTrainThreads) reinterpret_cast<uint4*>(sm + tr::AOP)[i] = z;
     const uint4* src = reinterpret_cast<const uint4*>(img);
-    for (int i = r; i < kImgBytes / 16; i += 128) reinterpret_cast<uint4*>(sm + tr::W)[i] = src[i];
+    for (int i = tid; i < kImgBytes / 16; i += kTrainThreads) reinterpret_cast<uint4*>(sm + tr::W)[i] = src[i];
     float* bias = reinterpret_cast<float*>(sm + tr::B);
-    if (r < kHid) bias[r] = P[ob2 + r];
-    if (r < kOut) bias[64 + r] = P[ob3 + r];
+    if (tid < kHid) bias[tid] = P[ob2 + tid];
+    if (tid < kOut) bias[64 + tid] = P[ob3 + tid];
   }
   __syncthreads();
-  store_bf16(sm + tr::BOP, 96, r, 128, 1.0f);
-  store_bf16(sm + tr::BOP3, 64, r, 128, 1.0f);
+  if (half == 0) {
+    store_bf16(sm + tr::BOP, 96, r, 128, 1.0f);
+    store_bf16(sm + tr::BOP3, 64, r, 128, 1.0f);
+  }
   const float* b2 = reinterpret_cast<const float*>(sm + tr::B);
   const float* b3 = b2 + 64;
   const uint32_t tb = tslot;
   Sync           sy{&mbar, 0u, &err};
 
-  // ---- the point ----
+  // ---- the point (half 0: its input row and target) ----
   const long j     = first + (long)blockIdx.x * 128 + r;
   const bool valid = j < n;
-  const long idx   = valid ? (long)((stride_a * j + offset_b) % n) : 0;
-  float      x[9], xs[9], t[6];
-  for (int q = 0; q < 9; q++) {
-    x[q]  = X[9 * idx + q];
-    xs[q] = x[q] * sc.in_scale;
+  float      t[6];
+  if (half == 0) {
+    const long idx = valid ? (long)((stride_a * j + offset_b) % n) : 0;
+    float      x[9], xs[9];
+    for (int q = 0; q < 9; q++) {
+      x[q]  = X[9 * idx + q];
+      xs[q] = x[q] * sc.in_scale;
+    }
+    {
+      float L[6];
+      base_part(x, sc.k_over_g, L);
+      const float g = gate(xs) * sc.res_scale;
+      for (int q = 0; q < 6; q++) t[q] = (Y[6 * idx + q] - L[q]) / g;
+    }
+    float row[kInX];
+    input_row(xs, row);
+    for (int k0 = 0; k0 < kInX; k0 += 8) store_chunk(sm + tr::X, r, k0, kInX, row + k0);
+    for (int q = 0; q < kInX; q++)
+      if (q < 10 || (q >= 16 && q < 25)) store_bf16(sm + tr::BOP, 64 + q, r, 128, row[q]);
   }
-  {
-    float L[6];
-    base_part(x, sc.k_over_g, L);
-    const float g = gate(xs) * sc.res_scale;
-    for (int q = 0; q < 6; q++) t[q] = (Y[6 * idx + q] - L[q]) / g;
-  }
-  float row[kInX];
-  input_row(xs, row);
-  for (int k0 = 0; k0 < kInX; k0 += 8) store_chunk(sm + tr::X, r, k0, kInX, row + k0);
-  for (int q = 0; q < kInX; q++)
-    if (q < 10 || (q >= 16 && q < 25)) store_bf16(sm + tr::BOP, 64 + q, r, 128, row[q]);
   publish_operands();
 
   // ---- forward ----
-  if (r == 0) {
+  if (tid == 0) {
     gemm(tb + tr::cZ1, sm + tr::X, kInX, sm + tr::W + kOffW1, kInX, kHid, kInX, false);
     mma_commit(&mbar);
   }
   if (!await_mma(sy)) goto cleanup;
   {
-    float z[64];
-    ld_row(tb, tr::cZ1, 4, z);
-    for (int q = 0; q < 64; q++) z[q] = act(z[q]);
-    for (int k0 = 0; k0 < 64; k0 += 8) store_chunk(sm + tr::A1, r, k0, kHid, z + k0);
-    for (int q = 0; q < 64; q++) store_bf16(sm + tr::BOP, q, r, 128, z[q]);
+    float z[32];
+    ld_row(tb, tr::cZ1 + c0, 2, z);
+    for (int q = 0; q < 32; q++) z[q] = act(z[q]);
+    for (int k0 = 0; k0 < 32; k0 += 8) store_chunk(sm + tr::A1, r, c0 + k0, kHid, z + k0);
+    for (int q = 0; q < 32; q++) store_bf16(sm + tr::BOP, c0 + q, r, 128, z[q]);
   }
   publish_operands();
-  if (r == 0) {
+  if (tid == 0) {
     gemm(tb + tr::cZ2, sm + tr::A1, kHid, sm + tr::W + kOffW2, kHid, kHid, kHid, false);
     mma_commit(&mbar);
   }
   if (!await_mma(sy)) goto cleanup;
   {
-    float z[64];
-    ld_row(tb, tr::cZ2, 4, z);
-    for (int q = 0; q < 64; q++) z[q] = act(z[q] + b2[q]);
-    for (int k0 = 0; k0 < 64; k0 += 8) store_chunk(sm + tr::A2, r, k0, kHid, z + k0);
-    for (int q = 0; q < 64; q++) store_bf16(sm + tr::BOP3, q, r, 128, z[q]);
+    float z[32];
+    ld_row(tb, tr::cZ2 + c0, 2, z);
+    for (int q = 0; q < 32; q++) z[q] = act(z[q] + b2[c0 + q]);
+    for (int k0 = 0; k0 < 32; k0 += 8) store_chunk(sm + tr::A2, r, c0 + k0, kHid, z + k0);
+    for (int q = 0; q < 32; q++) store_bf16(sm + tr::BOP3, c0 + q, r, 128, z[q]);
   }
   publish_operands();
-  if (r == 0) {
+  if (tid == 0) {
     gemm(tb + tr::cZ3, sm + tr::A2, kHid, sm + tr::W + kOffW3, kHid, kOutX, kHid, false);
     mma_commit(&mbar);
   }
   if (!await_mma(sy)) goto cleanup;
-  {
+  if (half == 0) {
     float z[16], g[16];
     ld_row(tb, tr::cZ3, 1, z);
     float lsum = 0.0f;
@@ -294,34 +307,34 @@ __global__ void __launch_bounds__(128) k_train(const float* __restrict__ X, cons
   }
   publish_operands();
   // ---- backward ----
-  if (r == 0) {
+  if (tid == 0) {
     gemm(tb + tr::cDA2, sm + tr::DZ3, kOutX, sm + tr::W + kOffW3t, kOutX, kHid, kOutX, false);
     mma_commit(&mbar);
   }
   if (!await_mma(sy)) goto cleanup;
   {
-    float da[64], z[64];
-    ld_row(tb, tr::cDA2, 4, da);
-    ld_row(tb, tr::cZ2, 4, z);
-    for (int q = 0; q < 64; q++) da[q] *= act_grad(z[q] + b2[q]);
-    for (int k0 = 0; k0 < 64; k0 += 8) store_chunk(sm + tr::DZ2, r, k0, kHid, da + k0);
-    for (int q = 0; q < 64; q++) store_bf16(sm + tr::AOP, q, r, 128, da[q]);
+    float da[32], z[32];
+    ld_row(tb, tr::cDA2 + c0, 2, da);
+    ld_row(tb, tr::cZ2 + c0, 2, z);
+    for (int q = 0; q < 32; q++) da[q] *= act_grad(z[q] + b2[c0 + q]);
+    for (int k0 = 0; k0 < 32; k0 += 8) store_chunk(sm + tr::DZ2, r, c0 + k0, kHid, da + k0);
+    for (int q = 0; q < 32; q++) store_bf16(sm + tr::AOP, c0 + q, r, 128, da[q]);
   }
   publish_operands();
-  if (r == 0) {
+  if (tid == 0) {
     gemm(tb + tr::cDA1, sm + tr::DZ2, kHid, sm + tr::W + kOffW2t, kHid, kHid, kHid, false);
     mma_commit(&mbar);
   }
   if (!await_mma(sy)) goto cleanup;
   {
-    float da[64], z[64];
-    ld_row(tb, tr::cDA1, 4, da);
-    ld_row(tb, tr::cZ1, 4, z);
-    for (int q = 0; q < 64; q++) store_bf16(sm + tr::AOP, 64 + q, r, 128, da[q] * act_grad(z[q]));
+    float da[32], z[32];
+    ld_row(tb, tr::cDA1 + c0, 2, da);
+    ld_row(tb, tr::cZ1 + c0, 2, z);
+    for (int q = 0; q < 32; q++) store_bf16(sm + tr::AOP, 64 + c0 + q, r, 128, da[q] * act_grad(z[q]));
   }
   publish_operands();
   // weight gradients: sums over the 128 points of the tile (K = points)
-  if (r == 0) {
+  if (tid == 0) {
     gemm(tb + tr::cGW, sm + tr::AOP, 128, sm + tr::BOP, 128, 112, 128, false);
     gemm(tb + tr::cGW3, sm + tr::AOP3, 128, sm + tr::BOP3, 128, 80, 128, false);
     mma_commit(&mbar);
@@ -329,32 +342,36 @@ __global__ void __launch_bounds__(128) k_train(const float* __restrict__ X, cons
   if (!await_mma(sy)) goto cleanup;
   {
     float* G = grad_partial + (long)blockIdx.x * kParams;
-    float  v[112];
-    ld_row(tb, tr::cGW, 7, v);
-    if (r < 64) {
-      for (int q = 0; q < 64; q++) G[oW2 + r * 64 + q] = v[q];
-      G[ob2 + r] = v[96];
-    } else {
-      const int o = r - 64;
-      for (int q = 0; q < 9; q++) G[oW1 + o * 9 + q] = v[64 + q] + v[64 + 16 + q];
-      G[ob1 + o] = v[64 + 9];
-    }
-    float w3[80];
-    ld_row(tb, tr::cGW3, 5, w3);
-    if (r < kOut) {
-      for (int q = 0; q < 64; q++) G[oW3 + r * 64 + q] = w3[q];
-      G[ob3 + r] = w3[64];
+    if (half == 0) {
+      // row r of the [112] block: W2 and b2 gradients (rows < 64), W1 and b1 (rows >= 64)
+      float v[112];
+      ld_row(tb, tr::cGW, 7, v);
+      if (r < 64) {
+        for (int q = 0; q < 64; q++) G[oW2 + r * 64 + q] = v[q];
+        G[ob2 + r] = v[96];
+      } else {
+        const int o = r - 64;
+        for (int q = 0; q < 9; q++) G[oW1 + o * 9 + q] = v[64 + q] + v[64 + 16 + q];
+        G[ob1 + o] = v[64 + 9];
+      }
+    } else if (warp == 4) {  // rows 0..31 of the W3 block: W3 and b3 gradients of rows < 6
+      float w3[80];
+      ld_row(tb, tr::cGW3, 5, w3);
+      if (r < kOut) {
+        for (int q = 0; q < 64; q++) G[oW3 + r * 64 + q] = w3[q];
+        G[ob3 + r] = w3[64];
+      }
     }
   }
   __syncthreads();
   for (int w = 64; w > 0; w >>= 1) {
-    if (r < w) red[r] += red[r + w];
+    if (tid < w) red[tid] += red[tid + w];
     __syncthreads();
   }
-  if (r == 0) loss_partial[blockIdx.x] = red[0];
+  if (tid == 0) loss_partial[blockIdx.x] = red[0];
 
 cleanup:
-  if (r == 0 && err) {
+  if (tid == 0 && err) {
     mbar_wait(sy.mbar, sy.phase ^ 1u);  // bounded: let a timed-out MMA drain before the columns are freed
     atomicOr(status, NSM_STATUS_TIMEOUT);
   }
@@ -542,7 +559,7 @@ cudaError_t launch_train(int tiles, const float* X, const float* Y, long n, long
                          const uint8_t* img, const float* P, const Scales& sc, float inv_batch, float* grad_partial,
                          float* loss_partial, int* status, cudaStream_t s)
 {
-  k_train<<<tiles, 128, tr::SMEM, s>>>(X, Y, n, first, stride_a, offset_b, img, P, sc, inv_batch, grad_partial,
+  k_train<<<tiles, kTrainThreads, tr::SMEM, s>>>(X, Y, n, first, stride_a, offset_b, img, P, sc, inv_batch, grad_partial,
                                        loss_partial, status);
   return cudaGetLastError();
 }

@@ -363,7 +363,8 @@ int nsm_get_profile(nsm_model* model, double* element_ms_total, int* element_lau
  * (NULL = zero), conn [E][8], dt_out one double.  It runs on `stream` (a
  * cudaStream_t of the current device; NULL = the default stream) and returns
  * without waiting.  With no elements dt_out receives the largest double, as
- * nsm_critical_time_step gives for an empty model.
+ * nsm_critical_time_step gives for an empty model; a connectivity entry outside
+ * [0, num_nodes) makes dt_out -1 (the element's coordinates are not read).
  * Its scratch is a fixed array inside this library sized for
  * NSM_NOALLOC_MAX_ELEMENTS elements (8 MiB per GPU, held until the process
  * exits); larger meshes are rejected with NSM_ERR_INVALID_ARGUMENT.  The first

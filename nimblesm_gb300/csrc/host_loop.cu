@@ -49,12 +49,24 @@ extern "C" int nsm_host_loop_steps(nsm_model* model, int num_steps, double* time
 {
   if (!model || !time_current || !mass || !u || !v || !a || !f_int || num_steps < 0)
     return nsm::set_last_error(NSM_ERR_INVALID_ARGUMENT, "nsm_host_loop_steps: null argument");
-  if (bcs)
-    for (int b = 0; b < bcs->num_bcs; b++)
+  const int N = nsm::model_num_nodes(model);
+  if (bcs && bcs->num_bcs > 0) {
+    if (!bcs->kind || !bcs->component || !bcs->value || !bcs->ptr || bcs->ptr[0] != 0)
+      return nsm::set_last_error(NSM_ERR_INVALID_ARGUMENT, "nsm_host_loop_steps: incomplete condition table");
+    for (int b = 0; b < bcs->num_bcs; b++) {
       if (bcs->kind[b] != NSM_BC_INITIAL_VELOCITY && bcs->kind[b] != NSM_BC_PRESCRIBED_VELOCITY &&
           bcs->kind[b] != NSM_BC_PRESCRIBED_DISPLACEMENT)
         return nsm::set_last_error(NSM_ERR_INVALID_ARGUMENT, "nsm_host_loop_steps: unknown condition kind");
-  const long n3   = 3L * nsm::model_num_nodes(model);
+      if (bcs->component[b] < 0 || bcs->component[b] > 2 || bcs->ptr[b + 1] < bcs->ptr[b])
+        return nsm::set_last_error(NSM_ERR_INVALID_ARGUMENT, "nsm_host_loop_steps: invalid condition");
+      if (bcs->ptr[b + 1] > bcs->ptr[b] && !bcs->nodes)
+        return nsm::set_last_error(NSM_ERR_INVALID_ARGUMENT, "nsm_host_loop_steps: null node list");
+      for (int k = bcs->ptr[b]; k < bcs->ptr[b + 1]; k++)
+        if (bcs->nodes[k] < 0 || bcs->nodes[k] >= N)
+          return nsm::set_last_error(NSM_ERR_INVALID_ARGUMENT, "nsm_host_loop_steps: node id out of range");
+    }
+  }
+  const long n3   = 3L * N;
   double     host = 0.0;
   using clk       = std::chrono::steady_clock;
   for (int s = 0; s < num_steps; s++) {

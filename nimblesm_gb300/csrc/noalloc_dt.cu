@@ -26,11 +26,14 @@
 #include "nsm_kernels.cuh"
 
 namespace {
-
 constexpr int kMaxBlocks = 1024;
+}  // namespace
 
 // The scratch: per-element time steps, then per-block minima.
-__device__ __align__(256) double g_noalloc_scratch[NSM_NOALLOC_MAX_ELEMENTS + kMaxBlocks];
+static __device__ __align__(256) double g_noalloc_scratch[NSM_NOALLOC_MAX_ELEMENTS + kMaxBlocks];
+
+namespace {
+
 
 // Device address of g_noalloc_scratch per device, looked up once per device
 // with that device current.  (In host code the symbol's name is only a
@@ -53,14 +56,25 @@ int invalid(const char* why)
   return nsm::set_last_error(NSM_ERR_INVALID_ARGUMENT, msg);
 }
 
-__global__ void k_elem_dt(int E, const int* __restrict__ conn, const double* __restrict__ coords,
+// An element whose connectivity names a node outside [0, N) reads no
+// coordinate and gets the time step -1, so that the minimum, and dt_out, is
+// negative: a bad mesh is reported instead of read out of bounds.
+__global__ void k_elem_dt(int N, int E, const int* __restrict__ conn, const double* __restrict__ coords,
                           const double* __restrict__ disp, double sound_speed, double* __restrict__ dt_elem)
 {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= E) return;
+  int ids[8];
+  for (int n = 0; n < 8; n++) {
+    ids[n] = conn[8L * e + n];
+    if (ids[n] < 0 || ids[n] >= N) {
+      dt_elem[e] = -1.0;
+      return;
+    }
+  }
   double x[8][3];
   for (int n = 0; n < 8; n++) {
-    const long id = conn[8L * e + n];
+    const long id = ids[n];
     for (int k = 0; k < 3; k++) x[n][k] = coords[3 * id + k] + (disp ? disp[3 * id + k] : 0.0);
   }
   double x_max = 0.0, y_max = 0.0, z_max = 0.0;  // maxima start at 0, as in the reference
@@ -138,7 +152,7 @@ extern "C" int nsm_critical_time_step_noalloc(int num_nodes, int num_elem, const
   if (blocks > kMaxBlocks) blocks = kMaxBlocks;
   if (num_elem > 0) {
     const double c = sqrt(bulk_modulus / density);
-    k_elem_dt<<<(num_elem + 127) / 128, 128, 0, s>>>(num_elem, conn, coords, displacement, c, dt_elem);
+    k_elem_dt<<<(num_elem + 127) / 128, 128, 0, s>>>(num_nodes, num_elem, conn, coords, displacement, c, dt_elem);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_error(e, "k_elem_dt launch");
     k_block_min<<<blocks, 256, 0, s>>>(num_elem, dt_elem, partial);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_error(e, "k_block_min launch");

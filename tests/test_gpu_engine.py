@@ -296,6 +296,11 @@ def test_host_loop_equals_device_loop():
         assert host_s > 0.0
     for k, key in (("u", "u"), ("v", "v"), ("a", "a"), ("f", "f_int")):
         assert np.array_equal(pins[k].array, g[key]), key
+    # a condition naming a node outside the model is refused before any step
+    p.node_sets["nodelist_1"] = np.append(p.node_sets["nodelist_1"], p.num_nodes).astype(np.int32)
+    with pytest.raises(E.EngineError, match="out of range"):
+        m.HostLoopSteps(1, t, (steps * dt) / steps, mass, pins["u"].array, pins["v"].array, pins["a"].array,
+                        pins["f"].array)
     m.close()
 
 

@@ -122,3 +122,31 @@ def test_noalloc_time_step_of_an_empty_mesh_is_the_largest_double():
         assert rc == 0, lib.nsm_last_error()
         torch.cuda.synchronize(dev)
         assert out.item() == np.finfo(np.float64).max
+
+
+def test_noalloc_time_step_reports_a_connectivity_outside_the_mesh():
+    """A connectivity entry naming a node outside [0, N) is not read: the
+    element's time step is -1, and so is the result, on two calls in a row."""
+    torch = pytest.importorskip("torch")
+    from nimblesm_gb300 import build as B
+    from nimblesm_gb300 import engine as E
+    from nimblesm_gb300.mesh import cube_problem
+
+    B.build()
+    lib = E.library()
+    p = cube_problem(4, jitter=0.2, seed=5)
+    conn = np.ascontiguousarray(p.conn, dtype=np.int32).copy()
+    conn[17, 3] = p.num_nodes  # one past the last node
+    dev = torch.device("cuda:0")
+    X = torch.from_numpy(np.ascontiguousarray(p.coords, dtype=np.float64).reshape(-1)).to(dev)
+    C = torch.from_numpy(conn.reshape(-1)).to(dev)
+    out = torch.empty(1, dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    for _ in range(2):
+        out.fill_(0.0)
+        rc = lib.nsm_critical_time_step_noalloc(p.num_nodes, p.num_elem, X.data_ptr(), None, C.data_ptr(),
+                                                p.density, p.bulk_modulus, out.data_ptr(), stream)
+        assert rc == 0, lib.nsm_last_error()
+        torch.cuda.synchronize(dev)
+        assert out.item() == -1.0
+

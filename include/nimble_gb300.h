@@ -436,10 +436,11 @@ int nsm_tc_selftest(int N, int K, const float* A, const float* B, float* D);
 
 /* Diagnostic of the failure path of the tensor-core waits: a kernel that
  * holds tensor memory waits on an mbarrier phase that nothing completes,
- * bounded by `polls` (1..100000) polls; *timed_out = 1 when the wait ran
- * out, after which the kernel freed its tensor memory and returned.  The
- * context stays usable. */
-int nsm_tc_wait_timeout_selftest(long polls, int* timed_out);
+ * bounded by `limit_us` (1..100000) microseconds of GPU time; *timed_out = 1
+ * when the wait ran out, after which the kernel freed its tensor memory and
+ * returned.  The context stays usable.  (Every tensor-core wait of the
+ * library is bounded the same way, at one second.) */
+int nsm_tc_wait_timeout_selftest(long limit_us, int* timed_out);
 
 /* Number of SMs of the device. */
 int nsm_device_sm_count(int device, int* count);

@@ -142,13 +142,6 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_element(ElementArgs a)
 // connectivity load nor the gather it addresses stalls the element math, and
 // nothing staged is held in registers.  Copy groups are per thread and each
 // thread reads only its own columns: no block barrier is needed.
-__device__ __forceinline__ void cp_async4(void* dst, const void* src)
-{
-  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
 // Per thread and slot: kStageValues floats (values 0..23 u, 24..47 X), then
 // 8 connectivity entries; column stride B.  Two slots, for the element being

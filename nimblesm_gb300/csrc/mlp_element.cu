@@ -15,7 +15,9 @@
 //     p with the sum for node p (21 shuffles, no shared memory).
 // The CTAs are persistent: each loads the operand images once and walks
 // chunks of 16 elements.  The three layers use the same 64 tensor-memory
-// columns in turn, so up to 8 CTAs fit the 512 columns of an SM.
+// columns in turn, so up to 8 CTAs fit the 512 columns of an SM.  The biases
+// of layers 2 and 3 are written into the accumulator by one extra K = 16 MMA
+// before the layer's own (bias_mma), so no thread adds a bias.
 // Points outside the training envelope take the plain neo-Hookean stress
 // (FP32) and are counted.
 #include <cuda_runtime.h>
@@ -36,8 +38,10 @@ namespace el {
 // the warp's own X rows (bytes [2048 w, 2048 w + 1024)).
 constexpr int A    = 0;
 constexpr int W    = A + 128 * kHid * 2;  // W1x, W2, W3x images
-constexpr int B    = W + kOffW2t;         // b2[64], b3[6]
-constexpr int SMEM = B + 512;
+constexpr int ONE  = W + kOffW2t;         // [8][16] ones in columns 0-2, read by every 8-row group (SBO 0)
+constexpr int B2b  = ONE + 256;           // [64][16]: three-term BF16 split of b2 in columns 0-2
+constexpr int B3b  = B2b + 2048;          // [16][16]: of b3 (rows 0-5)
+constexpr int SMEM = B3b + 512;
 constexpr int kStageWarp = 2048;          // bytes between the warps' staging areas
 constexpr uint32_t kCols = 64;
 constexpr int kElems = 16;                // elements per chunk
@@ -65,7 +69,7 @@ __device__ __forceinline__ void wait_commit(uint64_t* mbar, uint32_t& phase, int
 }
 
 // acc0: the first K-step accumulates onto what the columns hold (the bias
-// stored there by the previous epilogue) instead of overwriting it.
+// written there by bias_mma) instead of overwriting it.
 __device__ __forceinline__ void layer(uint32_t d, const uint8_t* a, int Ka, const uint8_t* b, int N, bool acc0 = false)
 {
   const uint32_t idesc = idesc_bf16_f32(128, N);
@@ -74,26 +78,36 @@ __device__ __forceinline__ void layer(uint32_t d, const uint8_t* a, int Ka, cons
              idesc, acc0 || ks > 0);
 }
 
+// Term t of the three-term BF16 split of an FP32 value: hi + mid + lo equals
+// v to 2^-27 relative, so the tensor core's FP32 sum 1 hi + 1 mid + 1 lo is v.
+__device__ __forceinline__ float bias_term(float v, int t)
+{
+  const float hi = __bfloat162float(__float2bfloat16_rn(v));
+  if (t == 0) return hi;
+  const float r1  = v - hi;
+  const float mid = __bfloat162float(__float2bfloat16_rn(r1));
+  return t == 1 ? mid : r1 - mid;
+}
+// D = ones * bias^T (one K = 16 step, overwriting D): every accumulator row
+// starts at the layer's FP32 bias, and the layer's MMAs accumulate onto it.
+// The A operand is one [8][16] core-matrix pair with ones in columns 0-2;
+// its stride between 8-row groups is 0, so all 128 rows read the same 256
+// bytes.  The B operand holds the bias's three-term split in columns 0-2.
+__device__ __forceinline__ void bias_mma(uint32_t d, const uint8_t* ones, const uint8_t* bias, int N)
+{
+  mma_bf16(d, smem_desc(smem_addr(ones), kLBO, 0), smem_desc(smem_addr(bias), kLBO, 256), idesc_bf16_f32(128, N), false);
+}
 // Hidden-layer epilogue: 64 accumulator columns of this thread's row ->
 // act(z) -> BF16 row r of the [128][64] activation tile, two columns per
-// packed FP32x2 operation.  With bias_next, each 16-column block of the
-// accumulator, once read, is overwritten with the next layer's bias, which
-// that layer's MMAs then accumulate onto: the bias costs 4 shared loads and
-// one tensor-memory store per 16 columns instead of a load and an add per
-// pair of columns.
-__device__ __forceinline__ void hidden_epilogue(uint32_t taddr, uint8_t* tile, int r, const float* bias_next)
+// packed FP32x2 operation.  (No bias is added here: the next layer's first
+// MMA writes it, see bias_mma.)
+__device__ __forceinline__ void hidden_epilogue(uint32_t taddr, uint8_t* tile, int r)
 {
 #pragma unroll
   for (int h = 0; h < 4; h++) {
     float z[16];
     tmem_ld16(taddr + 16 * h, z);
     tmem_wait_ld();
-    if (bias_next) {
-      float bn[16];
-#pragma unroll
-      for (int q = 0; q < 16; q += 4) *reinterpret_cast<float4*>(bn + q) = *reinterpret_cast<const float4*>(bias_next + 16 * h + q);
-      tmem_st16(taddr + 16 * h, bn);
-    }
 #pragma unroll
     for (int k0 = 0; k0 < 16; k0 += 8) {
       uint32_t w[4];
@@ -175,15 +189,16 @@ __global__ void __launch_bounds__(128, 6) k_element_mlp(ElementArgs a, MlpElemen
     // the layers' BF16 weight images
     const uint4* src = reinterpret_cast<const uint4*>(m.img);
     for (int i = r; i < kOffW2t / 16; i += 128) reinterpret_cast<uint4*>(sm + el::W)[i] = src[i];
-    float* bias = reinterpret_cast<float*>(sm + el::B);
-    if (r < kHid) bias[r] = m.P[ob2 + r];
-    if (r < kOut) bias[64 + r] = m.P[ob3 + r];
+    for (int i = r; i < 64 * 16; i += 128) {
+      const int n = i / 16, k = i % 16;
+      store_bf16(sm + el::B2b, n, k, 16, k < 3 ? bias_term(m.P[ob2 + n], k) : 0.0f);
+      if (n < 16) store_bf16(sm + el::B3b, n, k, 16, (k < 3 && n < kOut) ? bias_term(m.P[ob3 + n], k) : 0.0f);
+      if (n < 8) store_bf16(sm + el::ONE, n, k, 16, k < 3 ? 1.0f : 0.0f);
+    }
   }
   fence_before_sync();
   __syncthreads();
   fence_after_sync();
-  const float*   b2    = reinterpret_cast<const float*>(sm + el::B);
-  const float*   b3    = b2 + 64;
   const uint32_t tb    = tslot;
   const uint32_t taddr = tb + ((uint32_t)(warp * 32) << 16);
   uint8_t* const stage = sm + el::A + warp * el::kStageWarp;
@@ -264,21 +279,22 @@ __global__ void __launch_bounds__(128, 6) k_element_mlp(ElementArgs a, MlpElemen
     }
     id_next = node_of(chunk + gridDim.x);
     wait_commit(&mbar, phase, &err);
-    hidden_epilogue(taddr, sm + el::A, r, b2);  // leaves b2 in the columns for layer 2
-    tmem_wait_st();
+    hidden_epilogue(taddr, sm + el::A, r);
     // ---- layer 2 ----
     if (!publish(&err)) break;
     if (r == 0) {
+      bias_mma(tb, sm + el::ONE, sm + el::B2b, kHid);
       layer(tb, sm + el::A, kHid, sm + el::W + kOffW2, kHid, true);
       mma_commit(&mbar);
     }
     values_of(id_next, nv);
     wait_commit(&mbar, phase, &err);
-    hidden_epilogue(taddr, sm + el::A, r, nullptr);
+    hidden_epilogue(taddr, sm + el::A, r);
     // ---- layer 3 ----
     if (!publish(&err)) break;
     if (r == 0) {
-      layer(tb, sm + el::A, kHid, sm + el::W + kOffW3, kOutX);
+      bias_mma(tb, sm + el::ONE, sm + el::B3b, kOutX);
+      layer(tb, sm + el::A, kHid, sm + el::W + kOffW3, kOutX, true);
       mma_commit(&mbar);
     }
     wait_commit(&mbar, phase, &err);
@@ -294,7 +310,7 @@ __global__ void __launch_bounds__(128, 6) k_element_mlp(ElementArgs a, MlpElemen
         base_part(h, m.sc.k_over_g, L);
         const float g = gate(xs) * m.sc.res_scale;
 #pragma unroll
-        for (int q = 0; q < 6; q++) sig[q] = Gm * (L[q] + g * (z[q] + b3[q]));
+        for (int q = 0; q < 6; q++) sig[q] = Gm * fmaf(g, z[q], L[q]);
       } else {
         float H[3][3], C[3][3], J;
 #pragma unroll

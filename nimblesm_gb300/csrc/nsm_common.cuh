@@ -94,4 +94,16 @@ __host__ __device__ constexpr bool expr_is_unary(int code) { return code >= kExN
 
 inline int grid_for(long n, int block) { return (int)((n + block - 1) / block); }
 
+// 4-byte asynchronous copies global -> shared (per-thread copy groups), used
+// to stage the next element's nodal values while the current one computes.
+#ifdef __CUDACC__
+__device__ __forceinline__ void cp_async4(void* dst, const void* src)
+{
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+#endif
+
 }  // namespace nsm

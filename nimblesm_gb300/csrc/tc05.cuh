@@ -128,29 +128,64 @@ __device__ __forceinline__ void tmem_st16(uint32_t taddr, const float* v)
 }
 __device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 
+// 4 consecutive 32-bit columns of this thread's lane, written / read.
+__device__ __forceinline__ void tmem_st4(uint32_t taddr, const float* v)
+{
+  asm volatile("tcgen05.st.sync.aligned.32x32b.x4.b32 [%0], {%1,%2,%3,%4};" ::"r"(taddr), "f"(v[0]), "f"(v[1]), "f"(v[2]),
+               "f"(v[3])
+               : "memory");
+}
+__device__ __forceinline__ void tmem_ld4(uint32_t taddr, float* v)
+{
+  uint32_t r[4];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(taddr)
+               : "memory");
+#pragma unroll
+  for (int i = 0; i < 4; i++) v[i] = __uint_as_float(r[i]);
+}
+
 // ---- mbarrier ----
 __device__ __forceinline__ void mbar_init(uint64_t* mbar, uint32_t count)
 {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(mbar)), "r"(count) : "memory");
 }
+// One test of the phase parity.  A thread whose phase is not complete is
+// suspended in hardware until it completes or up to kSuspendNs (the
+// instruction's time hint) have passed, instead of spinning through issue
+// slots that the CTA's other warps need.
+constexpr uint32_t kSuspendNs = 1000000;
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* mbar, uint32_t phase)
 {
   uint32_t ok;
   asm volatile(
       "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
       "selp.b32 %0, 1, 0, p;\n\t}\n"
       : "=r"(ok)
-      : "r"(smem_addr(mbar)), "r"(phase)
+      : "r"(smem_addr(mbar)), "r"(phase), "n"(kSuspendNs)
       : "memory");
   return ok != 0;
 }
-// Bounded wait for the given phase parity; false after `limit` polls.
-__device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t phase, long limit = 4000000)
+__device__ __forceinline__ uint64_t global_ns()
 {
-  for (long i = 0; i < limit; i++)
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+// Bounded wait for the given phase parity: false once `limit_ns` of wall
+// time (the GPU's global timer) have passed without the phase completing.
+// The time is read only after a test failed, so a wait that completes at its
+// first test costs one instruction.
+__device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t phase, uint64_t limit_ns = 1000000000ull)
+{
+  if (mbar_try_wait(mbar, phase)) return true;
+  const uint64_t t0 = global_ns();
+  for (;;) {
     if (mbar_try_wait(mbar, phase)) return true;
-  return false;
+    if (global_ns() - t0 > limit_ns) return false;
+  }
 }
 
 }  // namespace tc

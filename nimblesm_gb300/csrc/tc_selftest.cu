@@ -70,9 +70,10 @@ __global__ void __launch_bounds__(128) k_tc_selftest(int N, int K, const float* 
 }
 
 // The failure path of every tensor-core wait: tensor memory held, a wait on
-// an mbarrier phase that nothing completes, bounded by `polls`; the kernel
-// records the timeout, frees its columns and returns.
-__global__ void __launch_bounds__(128) k_tc_wait_timeout(long polls, int* __restrict__ status)
+// an mbarrier phase that nothing completes, bounded by `limit_us`
+// microseconds; the kernel records the timeout, frees its columns and
+// returns.
+__global__ void __launch_bounds__(128) k_tc_wait_timeout(long limit_us, int* __restrict__ status)
 {
   __shared__ uint64_t mbar;
   __shared__ uint32_t tmem_slot;
@@ -85,7 +86,7 @@ __global__ void __launch_bounds__(128) k_tc_wait_timeout(long polls, int* __rest
   fence_before_sync();
   __syncthreads();
   fence_after_sync();
-  const bool done = mbar_wait(&mbar, 0, polls);  // no arrival is ever made
+  const bool done = mbar_wait(&mbar, 0, 1000ull * (uint64_t)limit_us);  // no arrival is ever made
   if (!done && tid == 0) atomicOr(status, 1);
   fence_before_sync();
   __syncthreads();
@@ -94,14 +95,14 @@ __global__ void __launch_bounds__(128) k_tc_wait_timeout(long polls, int* __rest
 
 }  // namespace
 
-extern "C" int nsm_tc_wait_timeout_selftest(long polls, int* timed_out)
+extern "C" int nsm_tc_wait_timeout_selftest(long limit_us, int* timed_out)
 {
-  if (!timed_out || polls < 1 || polls > 100000) return NSM_ERR_INVALID_ARGUMENT;
+  if (!timed_out || limit_us < 1 || limit_us > 100000) return NSM_ERR_INVALID_ARGUMENT;
   int* dS = nullptr;
   int  rc = NSM_OK, status = 0;
   if (cudaMalloc(&dS, sizeof(int)) != cudaSuccess || cudaMemset(dS, 0, sizeof(int)) != cudaSuccess) rc = NSM_ERR_CUDA;
   if (rc == NSM_OK) {
-    k_tc_wait_timeout<<<1, 128>>>(polls, dS);
+    k_tc_wait_timeout<<<1, 128>>>(limit_us, dS);
     if (cudaDeviceSynchronize() != cudaSuccess ||
         cudaMemcpy(&status, dS, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
       rc = NSM_ERR_CUDA;

@@ -198,8 +198,16 @@ int nsm_mlp_train(nsm_mlp* m, int epochs, int batch_tiles, double lr, double* fi
   const long   total       = steps_epoch * epochs;
   const double beta1 = 0.9, beta2 = 0.999, eps = 1e-8;
   uint64_t     s = 0x5EEDull + (uint64_t)m->adam_step;
-  std::vector<float> loss(batch_tiles);
-  double             epoch_loss = 0.0;
+  // the last epoch's per-tile losses stay on the device until the epoch ends
+  // (no per-step synchronisation), then are summed in step and tile order
+  std::vector<float> loss;
+  float*             d_epoch_loss = nullptr;
+  if (epochs > 0) MLP_CUDA(cudaMalloc(&d_epoch_loss, sizeof(float) * (size_t)steps_epoch * batch_tiles));
+  struct Free {
+    float* p;
+    ~Free() { if (p) cudaFree(p); }
+  } free_epoch_loss{d_epoch_loss};
+  double epoch_loss = 0.0;
   for (int ep = 0; ep < epochs; ep++) {
     // a fresh pseudo-random visiting order per epoch: j -> (a j + b) mod n, gcd(a, n) = 1
     long a;
@@ -215,17 +223,22 @@ int nsm_mlp_train(nsm_mlp* m, int epochs, int batch_tiles, double lr, double* fi
       const long   k     = m->adam_step + 1;
       const double frac  = total > 1 ? (double)(ep * steps_epoch + st) / (double)(total - 1) : 0.0;
       const double lr_t  = lr * (0.01 + 0.99 * 0.5 * (1.0 + std::cos(3.141592653589793 * frac)));
+      float* d_loss = ep == epochs - 1 ? d_epoch_loss + st * batch_tiles : m->d_loss;
       MLP_CUDA(launch_train(tiles, m->d_X, m->d_Y, m->n, first, a, b, m->d_img, m->d_P, m->sc, (float)(1.0 / pts),
-                            m->d_grad, m->d_loss, m->d_status, m->stream));
+                            m->d_grad, d_loss, m->d_status, m->stream));
       MLP_CUDA(launch_adam(tiles, m->d_grad, m->d_P, m->d_m1, m->d_m2, (float)lr_t, (float)beta1, (float)beta2,
                            (float)eps, (float)(1.0 - std::pow(beta1, (double)k)), (float)(1.0 - std::pow(beta2, (double)k)),
-                           m->stream));
-      MLP_CUDA(launch_images(m->d_P, m->d_img, m->stream));
+                           m->d_img, m->stream));
       m->adam_step++;
-      if (ep == epochs - 1) {
-        MLP_CUDA(cudaMemcpyAsync(loss.data(), m->d_loss, sizeof(float) * tiles, cudaMemcpyDeviceToHost, m->stream));
-        MLP_CUDA(cudaStreamSynchronize(m->stream));
-        for (int t = 0; t < tiles; t++) epoch_loss += loss[t];
+    }
+    if (ep == epochs - 1) {
+      loss.resize((size_t)steps_epoch * batch_tiles);
+      MLP_CUDA(cudaMemcpyAsync(loss.data(), d_epoch_loss, sizeof(float) * loss.size(), cudaMemcpyDeviceToHost, m->stream));
+      MLP_CUDA(cudaStreamSynchronize(m->stream));
+      for (long st = 0; st < steps_epoch; st++) {
+        const long pts   = std::min(batch, m->n - st * batch);
+        const int  tiles = (int)((pts + 127) / 128);
+        for (int t = 0; t < tiles; t++) epoch_loss += loss[(size_t)st * batch_tiles + t];
       }
     }
     r = check_status(m);

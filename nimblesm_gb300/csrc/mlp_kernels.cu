@@ -380,22 +380,56 @@ cleanup:
   if (warp == 0) tmem_dealloc(tb, tr::kCols);
 }
 
-// Deterministic reduction of the per-CTA gradients and an Adam step on the
-// FP32 master parameters.  Eight lanes share a parameter: lane j sums the
-// partials of CTAs j, j + 8, ... in order, and three butterfly steps combine
-// the eight sums in a fixed order, so every run gives the same bits while a
-// launch has eight times the loads in flight of one thread per parameter.
+// The operand-image entries of parameter i (the layout k_images writes), from
+// its value w.  The biases b2 and b3 have none (the kernels read them in
+// FP32), nor do the images' zero padding entries, which k_images wrote.
+__device__ __forceinline__ void store_images(int i, float w, uint8_t* __restrict__ img)
+{
+  if (i < ob1) {
+    const int n = (i - oW1) / kIn, k = (i - oW1) % kIn;
+    store_bf16(img + kOffW1, n, k, kInX, w);
+    store_bf16(img + kOffW1, n, k + 16, kInX, w);
+  } else if (i < oW2) {
+    store_bf16(img + kOffW1, i - ob1, 9, kInX, w);
+  } else if (i < ob2) {
+    const int n = (i - oW2) / kHid, k = (i - oW2) % kHid;
+    store_bf16(img + kOffW2, n, k, kHid, w);
+    store_bf16(img + kOffW2t, k, n, kHid, w);
+  } else if (i >= oW3 && i < ob3) {
+    const int n = (i - oW3) / kHid, k = (i - oW3) % kHid;
+    store_bf16(img + kOffW3, n, k, kHid, w);
+    store_bf16(img + kOffW3t, k, n, kOutX, w);
+  }
+}
+
+// Deterministic reduction of the per-CTA gradients, an Adam step on the FP32
+// master parameters, and the new parameters' BF16 operand-image entries.
+// Eight lanes share a parameter: lane j sums the partials of CTAs j, j + 8,
+// ... in order (loads issued four at a time ahead of the in-order sum), and
+// three butterfly steps combine the eight sums in a fixed order, so every
+// run gives the same bits while a launch has many loads in flight.
 constexpr int kAdamLanes = 8;
 __global__ void k_adam(int ncta, const float* __restrict__ grad_partial, float* __restrict__ P,
                        float* __restrict__ m1, float* __restrict__ m2, float lr, float beta1, float beta2,
-                       float eps, float bc1, float bc2)
+                       float eps, float bc1, float bc2, uint8_t* __restrict__ img)
 {
   const long t   = blockIdx.x * (long)blockDim.x + threadIdx.x;
   const int  i   = (int)(t / kAdamLanes), sub = (int)(t % kAdamLanes);
   const bool own = i < kParams;
   float      g   = 0.0f;
-  if (own)
-    for (int c = sub; c < ncta; c += kAdamLanes) g += grad_partial[(long)c * kParams + i];
+  if (own) {
+    const float* gp = grad_partial + i;
+    int          c  = sub;
+    for (; c + 3 * kAdamLanes < ncta; c += 4 * kAdamLanes) {
+      const float p0 = gp[(long)c * kParams], p1 = gp[(long)(c + kAdamLanes) * kParams],
+                  p2 = gp[(long)(c + 2 * kAdamLanes) * kParams], p3 = gp[(long)(c + 3 * kAdamLanes) * kParams];
+      g += p0;
+      g += p1;
+      g += p2;
+      g += p3;
+    }
+    for (; c < ncta; c += kAdamLanes) g += gp[(long)c * kParams];
+  }
 #pragma unroll
   for (int o = 1; o < kAdamLanes; o <<= 1) g += __shfl_xor_sync(0xffffffffu, g, o);
   if (!own || sub != 0) return;
@@ -403,7 +437,9 @@ __global__ void k_adam(int ncta, const float* __restrict__ grad_partial, float* 
   float b = beta2 * m2[i] + (1.0f - beta2) * g * g;
   m1[i]   = a;
   m2[i]   = b;
-  P[i] -= lr * (a / bc1) / (sqrtf(b / bc2) + eps);
+  const float w = P[i] - lr * (a / bc1) / (sqrtf(b / bc2) + eps);
+  P[i]          = w;
+  store_images(i, w, img);
 }
 
 __global__ void k_sum_gradient(int ncta, const float* __restrict__ grad_partial, float* __restrict__ g)
@@ -565,10 +601,10 @@ cudaError_t launch_train(int tiles, const float* X, const float* Y, long n, long
 }
 
 cudaError_t launch_adam(int ncta, const float* grad_partial, float* P, float* m1, float* m2, float lr, float beta1,
-                        float beta2, float eps, float bc1, float bc2, cudaStream_t s)
+                        float beta2, float eps, float bc1, float bc2, uint8_t* img, cudaStream_t s)
 {
   k_adam<<<(kParams * kAdamLanes + 255) / 256, 256, 0, s>>>(ncta, grad_partial, P, m1, m2, lr, beta1, beta2, eps,
-                                                             bc1, bc2);
+                                                             bc1, bc2, img);
   return cudaGetLastError();
 }
 

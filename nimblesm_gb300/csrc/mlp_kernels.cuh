@@ -20,8 +20,10 @@ cudaError_t launch_images(const float* P, uint8_t* img, cudaStream_t s);
 cudaError_t launch_train(int tiles, const float* X, const float* Y, long n, long first, long stride_a, long offset_b,
                          const uint8_t* img, const float* P, const Scales& sc, float inv_batch, float* grad_partial,
                          float* loss_partial, int* status, cudaStream_t s);
+// Sum of the per-CTA gradients, Adam step, and the updated parameters' BF16
+// operand-image entries (img, written in place).
 cudaError_t launch_adam(int ncta, const float* grad_partial, float* P, float* m1, float* m2, float lr, float beta1,
-                        float beta2, float eps, float bc1, float bc2, cudaStream_t s);
+                        float beta2, float eps, float bc1, float bc2, uint8_t* img, cudaStream_t s);
 cudaError_t launch_sum_gradient(int ncta, const float* grad_partial, float* g, cudaStream_t s);
 cudaError_t launch_predict(long n, const float* H, const uint8_t* img, const float* P, const Scales& sc, double K,
                            double G, double* sigma, int* fallback, int* status, cudaStream_t s);

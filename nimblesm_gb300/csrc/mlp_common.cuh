@@ -82,7 +82,7 @@ __device__ __forceinline__ float act_grad(float u)
   return fmaf(u, fmaf(-t, t, 1.0f), 1.0f + t);
 }
 
-// ---- packed FP32x2 arithmetic (add/mul/fma .rn.f32x2, sm_100 and later) ----
+// ---- packed FP32x2 arithmetic (fma.rn.f32x2, sm_100 and later) ----
 // Each lane is the IEEE round-to-nearest FP32 operation, so a packed
 // evaluation is bitwise the scalar one in the same order.
 using f32x2 = unsigned long long;
@@ -93,18 +93,6 @@ __device__ __forceinline__ f32x2 f2_pack(float x, float y)
   return r;
 }
 __device__ __forceinline__ void f2_unpack(f32x2 v, float& x, float& y) { asm("mov.b64 {%0, %1}, %2;" : "=f"(x), "=f"(y) : "l"(v)); }
-__device__ __forceinline__ f32x2 f2_add(f32x2 a, f32x2 b)
-{
-  f32x2 d;
-  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-  return d;
-}
-__device__ __forceinline__ f32x2 f2_mul(f32x2 a, f32x2 b)
-{
-  f32x2 d;
-  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-  return d;
-}
 __device__ __forceinline__ f32x2 f2_fma(f32x2 a, f32x2 b, f32x2 c)
 {
   f32x2 d;

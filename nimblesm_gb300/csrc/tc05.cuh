@@ -116,36 +116,6 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v)
 }
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
-// 16 consecutive 32-bit columns of this thread's lane written from registers
-// (32x32b shape, the lanes as in tmem_ld16).
-__device__ __forceinline__ void tmem_st16(uint32_t taddr, const float* v)
-{
-  asm volatile(
-      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(taddr),
-      "f"(v[0]), "f"(v[1]), "f"(v[2]), "f"(v[3]), "f"(v[4]), "f"(v[5]), "f"(v[6]), "f"(v[7]), "f"(v[8]), "f"(v[9]),
-      "f"(v[10]), "f"(v[11]), "f"(v[12]), "f"(v[13]), "f"(v[14]), "f"(v[15])
-      : "memory");
-}
-__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
-
-// 4 consecutive 32-bit columns of this thread's lane, written / read.
-__device__ __forceinline__ void tmem_st4(uint32_t taddr, const float* v)
-{
-  asm volatile("tcgen05.st.sync.aligned.32x32b.x4.b32 [%0], {%1,%2,%3,%4};" ::"r"(taddr), "f"(v[0]), "f"(v[1]), "f"(v[2]),
-               "f"(v[3])
-               : "memory");
-}
-__device__ __forceinline__ void tmem_ld4(uint32_t taddr, float* v)
-{
-  uint32_t r[4];
-  asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
-               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
-               : "r"(taddr)
-               : "memory");
-#pragma unroll
-  for (int i = 0; i < 4; i++) v[i] = __uint_as_float(r[i]);
-}
-
 // ---- mbarrier ----
 __device__ __forceinline__ void mbar_init(uint64_t* mbar, uint32_t count)
 {

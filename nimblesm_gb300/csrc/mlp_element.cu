@@ -97,19 +97,21 @@ __device__ __forceinline__ void bias_mma(uint32_t d, const uint8_t* ones, const 
 {
   mma_bf16(d, smem_desc(smem_addr(ones), kLBO, 0), smem_desc(smem_addr(bias), kLBO, 256), idesc_bf16_f32(128, N), false);
 }
-// Hidden-layer epilogue: 64 accumulator columns of this thread's row ->
-// act(z) -> BF16 row r of the [128][64] activation tile, two columns per
-// packed FP32x2 operation.  (No bias is added here: the next layer's first
-// MMA writes it, see bias_mma.)
+// Hidden-layer epilogue: 64 accumulator columns of this thread's row, read as
+// two 32-column halves (two tensor-memory loads per wait) -> act(z) -> BF16
+// row r of the [128][64] activation tile, two columns per packed FP32x2
+// operation.  (No bias is added here: the next layer's first MMA writes it,
+// see bias_mma.)
 __device__ __forceinline__ void hidden_epilogue(uint32_t taddr, uint8_t* tile, int r)
 {
 #pragma unroll
-  for (int h = 0; h < 4; h++) {
-    float z[16];
+  for (int h = 0; h < 4; h += 2) {
+    float z[32];
     tmem_ld16(taddr + 16 * h, z);
+    tmem_ld16(taddr + 16 * h + 16, z + 16);
     tmem_wait_ld();
 #pragma unroll
-    for (int k0 = 0; k0 < 16; k0 += 8) {
+    for (int k0 = 0; k0 < 32; k0 += 8) {
       uint32_t w[4];
 #pragma unroll
       for (int j = 0; j < 4; j++) w[j] = act_bf16(f2_pack(z[k0 + 2 * j], z[k0 + 2 * j + 1]));

@@ -206,6 +206,20 @@ __global__ void __launch_bounds__(kTrainThreads) k_train(const float* __restrict
   const int           tid = threadIdx.x, warp = tid >> 5, r = tid & 127, half = tid >> 7;
   const int           c0  = 32 * half;  // this thread's first column in the 64-column epilogues
 
+  // The point's pair (half 0) is gathered first, from its row of the epoch's
+  // visiting order, so that the loads' latency passes while the operand
+  // regions below are set up.
+  const long j     = first + (long)blockIdx.x * 128 + r;
+  const bool valid = j < n;
+  float      x[9], y[6];
+  if (half == 0) {
+    const long idx = valid ? (long)((stride_a * j + offset_b) % n) : 0;
+#pragma unroll
+    for (int q = 0; q < 9; q++) x[q] = X[9 * idx + q];
+#pragma unroll
+    for (int q = 0; q < 6; q++) y[q] = Y[6 * idx + q];
+  }
+
   if (warp == 0) {
     tmem_alloc(&tslot, tr::kCols);
     tmem_relinquish();
@@ -235,21 +249,15 @@ __global__ void __launch_bounds__(kTrainThreads) k_train(const float* __restrict
   Sync           sy{&mbar, 0u, &err};
 
   // ---- the point (half 0: its input row and target) ----
-  const long j     = first + (long)blockIdx.x * 128 + r;
-  const bool valid = j < n;
-  float      t[6];
+  float t[6];
   if (half == 0) {
-    const long idx = valid ? (long)((stride_a * j + offset_b) % n) : 0;
-    float      x[9], xs[9];
-    for (int q = 0; q < 9; q++) {
-      x[q]  = X[9 * idx + q];
-      xs[q] = x[q] * sc.in_scale;
-    }
+    float xs[9];
+    for (int q = 0; q < 9; q++) xs[q] = x[q] * sc.in_scale;
     {
       float L[6];
       base_part(x, sc.k_over_g, L);
       const float g = gate(xs) * sc.res_scale;
-      for (int q = 0; q < 6; q++) t[q] = (Y[6 * idx + q] - L[q]) / g;
+      for (int q = 0; q < 6; q++) t[q] = (y[q] - L[q]) / g;
     }
     float row[kInX];
     input_row(xs, row);
